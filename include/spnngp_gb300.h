@@ -1,0 +1,196 @@
+/*
+ * spnngp_gb300 -- C ABI of the GB300 (sm_103a) NNGP hot path.
+ *
+ * Every entry point below replaces one native routine of the R package spNNGP
+ * (v1.0.1) that its R front-ends reach through .Call; the comment on each
+ * names the routine and its file:line in the spNNGP source tree.  The
+ * conventions are the reference's own:
+ *   - matrices are column-major double, indices 0-based int32;
+ *   - the packed neighbor arrays use nnIndxLU = [offsets (n) | counts (n)] and
+ *     hold nIndx = (1+m)/2*m + (n-m-1)*m entries (src/rNNGP.cpp:218);
+ *   - covModel: 0 exponential, 1 spherical, 2 matern, 3 gaussian (R/spNNGP.R:172);
+ *   - response theta = (sigma^2, tau^2, phi[, nu]) (src/rNNGP.cpp:182-190);
+ *     conjugate thetaAlpha is nTheta x g with rows (phi, alpha[, nu])
+ *     (src/cNNGP.cpp:147-151, R/spConjNNGP.R:207-210);
+ *   - data arrive already permuted into the NNGP order.
+ * The "host" entry points take host pointers (exactly what the reference's
+ * .Call receives) and copy to and from the device inside the call; the
+ * "_dev" entry points take device pointers for data kept resident in HBM.
+ *
+ * Errors: every call returns an nngp_status.  NNGP_ERR_NOT_SPD carries the
+ * 0-based location (or prediction point) whose neighborhood covariance had a
+ * non-positive pivot, retrievable with nngp_error_location(); the reference
+ * raises Rf_error("c++ Rf_error: dpotrf failed") in that case
+ * (src/rNNGP.cpp:86).  Nothing falls back to the CPU: without a usable GB300
+ * every call returns NNGP_ERR_CUDA.
+ *
+ * Random numbers are never drawn inside the library.  The MCMC routines read
+ * host-fed streams of standard normals and uniforms in the order the
+ * reference consumes R's generator, so an R binding fills them with
+ * norm_rand()/unif_rand() and reproduces the reference's chain draw for draw.
+ */
+#ifndef SPNNGP_GB300_H
+#define SPNNGP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nngp_ctx nngp_ctx;
+
+typedef enum {
+  NNGP_OK = 0,
+  NNGP_ERR_ARG = 1,         /* invalid argument (sizes, covModel, m out of range ...) */
+  NNGP_ERR_CUDA = 2,        /* CUDA runtime error or no usable device */
+  NNGP_ERR_NOT_SPD = 3,     /* a neighborhood covariance (or the p x p Gram) is not SPD */
+  NNGP_ERR_NO_MEMORY = 4,   /* device allocation failed */
+  NNGP_ERR_STREAM = 5       /* a host-fed random stream is too short */
+} nngp_status;
+
+typedef enum {
+  NNGP_FP64 = 0,  /* plain FP64 throughout */
+  NNGP_FP32R = 1  /* FP32 covariance build + Cholesky, one FP64-residual refinement of B */
+} nngp_precision;
+
+/* ---------------------------------------------------------------- context */
+int nngp_create(int device, nngp_ctx **ctx);
+void nngp_destroy(nngp_ctx *ctx);
+const char *nngp_error_message(const nngp_ctx *ctx);
+int64_t nngp_error_location(const nngp_ctx *ctx);
+/* cudaStream_t to launch on (NULL = the context's own stream). */
+int nngp_set_stream(nngp_ctx *ctx, void *stream);
+void *nngp_get_stream(const nngp_ctx *ctx);
+int nngp_synchronize(nngp_ctx *ctx);
+/* Kernels this library launched since the counter was last reset. */
+int64_t nngp_launch_count(const nngp_ctx *ctx);
+void nngp_reset_launch_count(nngp_ctx *ctx);
+/* Largest neighbor count the kernels accept (m <= this). */
+int nngp_max_neighbors(void);
+int64_t nngp_n_indx(int n, int m);
+
+/* ---------------------------------------------------------- neighbor search */
+
+/* Ordered kNN by the mean-distance code-book search: for every location the
+ * m nearest predecessors, bit-exact with the reference including its tie
+ * order.  Replaces mkNNIndxCB (src/nn.cpp:213-258, called from R/nn.R:71);
+ * outputs are written in place as the reference does. */
+int nngp_mkNNIndxCB(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
+                    double *nnDist, int *nnIndxLU);
+
+/* Ordered kNN by exhaustive scan in index order; same result contract as the
+ * reference's brute-force search.  Replaces mkNNIndx (src/nn.cpp:63-111,
+ * called from R/nn.R:45). */
+int nngp_mkNNIndx(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
+                  double *nnDist, int *nnIndxLU);
+
+/* Reverse neighbor index: uIndx lists, for each location, the locations that
+ * have it as a neighbor (increasing order for searchType 0 and 2, decreasing
+ * for 1), uIndxLU = [offsets | counts], uiIndx the position inside each such
+ * list.  Replaces mkUIndx (src/nn.cpp:25-56, src/util.cpp:72-185, called from
+ * R/nn.R:19). */
+int nngp_mkUIndx(nngp_ctx *ctx, int n, int m, const int *nnIndx, int *uIndx, int *uIndxLU,
+                 int *uiIndx, const int *nnIndxLU, int searchType);
+
+/* Unconstrained exact kNN of n0 prediction points among n training points,
+ * nnIdx n0 x k column-major 0-based, nnDist the Euclidean distances (may be
+ * NULL); ascending distance, ties by smaller training index.  Replaces the
+ * RANN::nn2 calls at R/spConjNNGP.R:158,311 and R/generics.R:642. */
+int nngp_nn2(nngp_ctx *ctx, int n, const double *coords, int n0, const double *coords0, int k,
+             int *nnIdx, double *nnDist);
+
+/* -------------------------------------------------------------- B, F and Q */
+
+/* B_i = C_N(i)^-1 c_i and F_i = sigma^2 + tau^2 - B_i'c_i for every location,
+ * and logDet = sum_i log F_i.  theta = (sigma^2, tau^2, phi[, nu]).
+ * Replaces updateBF (src/rNNGP.cpp:46-101). */
+int nngp_updateBF(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                  const int *nnIndxLU, int covModel, const double *theta, int precision,
+                  double *B, double *F, double *logDet);
+
+/* Conjugate form: sigma^2 = 1, nugget alpha.  Replaces updateConjBF
+ * (src/cNNGP.cpp:24-69). */
+int nngp_updateConjBF(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                      const int *nnIndxLU, int covModel, double phi, double alpha, double nu,
+                      int precision, double *B, double *F);
+
+/* q = u'(I-B)'F^-1(I-B)v.  Replaces Q (src/util.cpp:261-280). */
+int nngp_Q(nngp_ctx *ctx, const double *B, const double *F, const double *u, const double *v,
+           int n, const int *nnIndx, const int *nnIndxLU, double *q);
+
+/* Fused likelihood pass: for the nv columns V = [X y] (n x nv, column-major),
+ * logDet = sum log F_i and gram = V'(I-B)'F^-1(I-B)V (nv x nv, column-major,
+ * symmetric) without writing B or F.  One call replaces one updateBF plus the
+ * p(p+3)/2 + 1 Q calls of src/rNNGP.cpp:255-259,281-286 and src/cNNGP.cpp:224-245. */
+int nngp_loglik_gram(nngp_ctx *ctx, int n, int m, int nv, const double *coords,
+                     const int *nnIndx, const int *nnIndxLU, const double *V, int covModel,
+                     const double *theta, int precision, double *logDet, double *gram);
+
+/* ------------------------------------------------------------ model drivers */
+
+/* Response-model Metropolis-within-Gibbs.  Argument meaning follows .Call
+ * ("rNNGP", ...) (R/spNNGP.R:401-405, src/rNNGP.cpp:105-109): thetaStarting and
+ * tuning are (sigma^2, tau^2, phi[, nu]).  normals/unifs are the host-fed
+ * streams, consumed per iteration as: p normals for beta, n for the replicate
+ * when repIndx[s] != 0, then one per proposal (phi, sigma^2, tau^2[, nu]) whose
+ * tuning is non-zero, then one uniform.  Outputs betaSamples p x nSamples,
+ * thetaSamples nTheta x nSamples, repSamples n x nRep (may be NULL when nRep
+ * == 0), *nAccept.  Replaces rNNGP (src/rNNGP.cpp:103-421). */
+int nngp_rNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, int m,
+               const double *coords, int covModel, const int *nnIndx, const int *nnIndxLU,
+               const double *sigmaSqIG, const double *tauSqIG, const double *phiUnif,
+               const double *nuUnif, const double *betaStarting, const double *thetaStarting,
+               const double *tuning, int nSamples, int nRep, const int *repIndx,
+               const double *normals, int64_t nNormals, const double *unifs, int64_t nUnifs,
+               int precision, double *betaSamples, double *thetaSamples, double *repSamples,
+               int *nAccept);
+
+/* Conjugate NNGP over g parameter sets with prediction at n0 points.
+ * Argument meaning follows .Call("cNNGP", ...) (R/spConjNNGP.R:336-338,
+ * src/cNNGP.cpp:73-75).  Outputs betaHat p x g, ab 2 x g, bBInv p*p x g (lower
+ * triangle, upper zero), bb p x g, y0Hat and y0HatVar n0 x g (may be NULL when
+ * n0 == 0).  Replaces cNNGP (src/cNNGP.cpp:73-358). */
+int nngp_cNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n,
+               const double *coords, const double *thetaAlpha, const int *nnIndx,
+               const int *nnIndxLU, const double *X0, const double *coords0, int n0,
+               const int *nnIndx0, int g, int m, const double *sigmaSqIG, int covModel,
+               int precision, double *betaHat, double *ab, double *bBInv, double *bb,
+               double *y0Hat, double *y0HatVar);
+
+/* Posterior predictive draws at q points for nSamples kept samples.  betaSamples
+ * p x nSamples, thetaSamples nTheta x nSamples, z q*nSamples standard normals
+ * with z[i*nSamples + s] used for (point i, sample s).  Output y0 q x nSamples.
+ * Replaces rNNGPPredict (src/rNNGPPredict.cpp:25-223). */
+int nngp_rNNGPPredict(nngp_ctx *ctx, const double *X, const double *y, const double *coords,
+                      int n, int p, int m, const double *X0, const double *coords0, int q,
+                      const int *nnIndx0, const double *betaSamples, const double *thetaSamples,
+                      int nSamples, int covModel, const double *z, int precision, double *y0);
+
+/* Replicated data y_rep = X beta_s + v_s, v_s drawn by the sequential NNGP
+ * recurrence at every sample's theta; beta is nSamples x p, theta nTheta x
+ * nSamples, normals n*nSamples consumed location by location, sample by sample.
+ * Output yRep n x nSamples.  Replaces rNNGPReplicated
+ * (src/rNNGPReplicated.cpp:74-244). */
+int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m,
+                         const double *coords, int covModel, const int *nnIndx,
+                         const int *nnIndxLU, const double *beta, const double *theta,
+                         int nSamples, const double *normals, int precision, double *yRep);
+
+/* ----------------------------------------------- device-resident variants
+ * Same contracts as above; every pointer is device memory and the call is
+ * asynchronous on the context stream (status and logDet/gram are available
+ * after nngp_synchronize).  Coordinates are n x 2 column-major. */
+int nngp_updateBF_dev(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                      const int *nnIndxLU, int covModel, const double *theta, int precision,
+                      double *B, double *F, double *logDet);
+int nngp_loglik_gram_dev(nngp_ctx *ctx, int n, int m, int nv, const double *coords,
+                         const int *nnIndx, const int *nnIndxLU, const double *V, int covModel,
+                         const double *theta, int precision, double *logDet, double *gram);
+int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
+                        double *nnDist, int *nnIndxLU);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

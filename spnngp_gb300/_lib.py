@@ -1,0 +1,175 @@
+"""ctypes binding of libspnngp_gb300.so (the C ABI declared in include/spnngp_gb300.h).
+
+There is no CPU implementation behind this module: if the library is missing or
+no GB300 is usable, calls raise.  Arrays are passed as numpy buffers
+(host entry points) or as raw device pointers (``*_dev`` entry points).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libspnngp_gb300.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_i64 = C.c_int64
+
+# status codes (include/spnngp_gb300.h)
+NNGP_OK, NNGP_ERR_ARG, NNGP_ERR_CUDA, NNGP_ERR_NOT_SPD, NNGP_ERR_NO_MEMORY, NNGP_ERR_STREAM = range(6)
+FP64, FP32R = 0, 1
+
+_SIGNATURES = {
+    "nngp_create": (_i, [_i, C.POINTER(_vp)]),
+    "nngp_destroy": (None, [_vp]),
+    "nngp_error_message": (C.c_char_p, [_vp]),
+    "nngp_error_location": (_i64, [_vp]),
+    "nngp_set_stream": (_i, [_vp, _vp]),
+    "nngp_get_stream": (_vp, [_vp]),
+    "nngp_synchronize": (_i, [_vp]),
+    "nngp_launch_count": (_i64, [_vp]),
+    "nngp_reset_launch_count": (None, [_vp]),
+    "nngp_max_neighbors": (_i, []),
+    "nngp_n_indx": (_i64, [_i, _i]),
+    "nngp_mkNNIndxCB": (_i, [_vp, _i, _i, _dp, _ip, _dp, _ip]),
+    "nngp_mkNNIndx": (_i, [_vp, _i, _i, _dp, _ip, _dp, _ip]),
+    "nngp_mkUIndx": (_i, [_vp, _i, _i, _ip, _ip, _ip, _ip, _ip, _i]),
+    "nngp_nn2": (_i, [_vp, _i, _dp, _i, _dp, _i, _ip, _dp]),
+    "nngp_updateBF": (_i, [_vp, _i, _i, _dp, _ip, _ip, _i, _dp, _i, _dp, _dp, _dp]),
+    "nngp_updateConjBF": (_i, [_vp, _i, _i, _dp, _ip, _ip, _i, _d, _d, _d, _i, _dp, _dp]),
+    "nngp_Q": (_i, [_vp, _dp, _dp, _dp, _dp, _i, _ip, _ip, _dp]),
+    "nngp_loglik_gram": (_i, [_vp, _i, _i, _i, _dp, _ip, _ip, _dp, _i, _dp, _i, _dp, _dp]),
+    "nngp_rNNGP": (_i, [_vp, _dp, _dp, _i, _i, _i, _dp, _i, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                        _i, _i, _ip, _dp, _i64, _dp, _i64, _i, _dp, _dp, _dp, _ip]),
+    "nngp_cNNGP": (_i, [_vp, _dp, _dp, _i, _i, _dp, _dp, _ip, _ip, _dp, _dp, _i, _ip, _i, _i, _dp, _i, _i,
+                        _dp, _dp, _dp, _dp, _dp, _dp]),
+    "nngp_rNNGPPredict": (_i, [_vp, _dp, _dp, _dp, _i, _i, _i, _dp, _dp, _i, _ip, _dp, _dp, _i, _i, _dp, _i,
+                               _dp]),
+    "nngp_rNNGPReplicated": (_i, [_vp, _dp, _i, _i, _i, _dp, _i, _ip, _ip, _dp, _dp, _i, _dp, _i, _dp]),
+    # device-resident variants: every array argument is a device pointer (theta stays on the host)
+    "nngp_updateBF_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp, _vp]),
+    "nngp_loglik_gram_dev": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp]),
+    "nngp_mkNNIndxCB_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
+}
+
+
+class NNGPError(RuntimeError):
+    """A non-zero status from the library; ``location`` is the failing location or -1."""
+
+    def __init__(self, status: int, message: str, location: int = -1):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+        self.location = location
+
+
+class _Lib:
+    def __init__(self, path: str = LIB_PATH):
+        if not os.path.exists(path):
+            raise ImportError(
+                f"{path} is not built; build it with `python -m spnngp_gb300.build` (requires nvcc)")
+        self.path = path
+        self.cdll = C.CDLL(path)
+        self._fns = {}
+
+    def fn(self, name: str):
+        f = self._fns.get(name)
+        if f is None:
+            f = getattr(self.cdll, name)
+            res, args = _SIGNATURES[name]
+            f.restype = res
+            f.argtypes = args
+            self._fns[name] = f
+        return f
+
+
+_LIB = None
+_LIB_LOCK = threading.Lock()
+
+
+def lib() -> _Lib:
+    global _LIB
+    with _LIB_LOCK:
+        if _LIB is None:
+            _LIB = _Lib()
+        return _LIB
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray):
+    return a.ctypes.data_as(_ip)
+
+
+def f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One library context (device, stream, scratch).  Not thread-safe; use one per thread."""
+
+    def __init__(self, device: int = 0):
+        self._lib = lib()
+        h = _vp()
+        st = self._lib.fn("nngp_create")(device, C.byref(h))
+        if st != NNGP_OK:
+            raise NNGPError(st, f"could not create a context on CUDA device {device} (no usable GB300?)")
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.fn("nngp_destroy")(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def call(self, name: str, *args) -> int:
+        st = self._lib.fn(name)(self.handle, *args)
+        if st != NNGP_OK:
+            msg = self._lib.fn("nngp_error_message")(self.handle)
+            loc = self._lib.fn("nngp_error_location")(self.handle)
+            raise NNGPError(st, (msg or b"").decode(), int(loc))
+        return st
+
+    def set_stream(self, stream_handle: int | None):
+        self._lib.fn("nngp_set_stream")(self.handle, stream_handle or None)
+
+    def synchronize(self):
+        self.call("nngp_synchronize")
+
+    @property
+    def launches(self) -> int:
+        return int(self._lib.fn("nngp_launch_count")(self.handle))
+
+    def reset_launches(self):
+        self._lib.fn("nngp_reset_launch_count")(self.handle)
+
+
+_DEFAULT = None
+
+
+def default_context() -> Context:
+    global _DEFAULT
+    if _DEFAULT is None:
+        _DEFAULT = Context(0)
+    return _DEFAULT
+
+
+def n_indx(n: int, m: int) -> int:
+    return int((1 + m) / 2 * m + (n - m - 1) * m)

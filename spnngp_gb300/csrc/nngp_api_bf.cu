@@ -1,0 +1,291 @@
+// C-ABI entry points of the B/F pass: updateBF / updateConjBF (src/rNNGP.cpp:46-101,
+// src/cNNGP.cpp:24-69), Q (src/util.cpp:261-280) and the fused likelihood/Gram pass.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include "nngp_internal.h"
+
+namespace {
+
+__global__ void interleave_kernel(const double *__restrict__ cm, int n, double *__restrict__ xy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    xy[2 * i] = cm[i];
+    xy[2 * i + 1] = cm[n + i];
+  }
+}
+
+// col-major n x nv -> row-major n x nv
+__global__ void to_row_major_kernel(const double *__restrict__ cm, int n, int nv, double *__restrict__ rm) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long)n * nv) {
+    const int i = (int)(t / nv), v = (int)(t % nv);
+    rm[t] = cm[(size_t)v * n + i];
+  }
+}
+
+// Q: per-tile sums of (u_i - B_i u_N)(v_i - B_i v_N) / F_i.
+__global__ void q_kernel(const double *__restrict__ B, const double *__restrict__ F,
+                         const double *__restrict__ u, const double *__restrict__ v, int n,
+                         const int *__restrict__ nnIndx, const int *__restrict__ nnLU,
+                         double *__restrict__ partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double q = 0.0;
+  if (i < n) {
+    double a = 0.0, b = 0.0;
+    const int off = nnLU[i], cnt = nnLU[n + i];
+    for (int j = 0; j < cnt; j++) {
+      const double w = B[off + j];
+      const int k = nnIndx[off + j];
+      a += w * u[k];
+      b += w * v[k];
+    }
+    q = (u[i] - a) * (v[i] - b) / F[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+  __shared__ double wb[8];
+  if ((threadIdx.x & 31) == 0) wb[threadIdx.x >> 5] = q;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += wb[w];
+    partial[blockIdx.x] = s;
+  }
+}
+
+__global__ void sum_kernel(const double *__restrict__ x, int cnt, double *__restrict__ out) {
+  __shared__ double s[256];
+  double a = 0.0;
+  for (int t = threadIdx.x; t < cnt; t += 256) a += x[t];
+  s[threadIdx.x] = a;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = s[0];
+}
+
+int check_common(nngp_ctx *ctx, int n, int m, int covModel) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (n < 1 || m < 1 || m > NNGP_MAX_M) return nngp_fail(ctx, NNGP_ERR_ARG, "n >= 1 and 1 <= m <= 32 required");
+  if (n < m) return nngp_fail(ctx, NNGP_ERR_ARG, "n must be at least m (the packed neighbor layout needs n >= m)");
+  if (covModel < 0 || covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+  return NNGP_OK;
+}
+
+CovParams make_params(int covModel, double sigmaSq, double tauSq, double phi, double nu) {
+  CovParams c{};
+  c.model = covModel;
+  c.sigmaSq = sigmaSq;
+  c.tauSq = tauSq;
+  c.phi = phi;
+  c.nu = nu;
+  cov_prepare(c);
+  return c;
+}
+
+// Single-evaluation pass on resident data.  coords are n x 2 column-major (device).
+int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_coords_cm,
+               const int *d_nnIndx, const int *d_nnLU, const double *d_V_cm, const CovParams &cp,
+               int precision, double *d_B, double *d_F, double *h_out) {
+  if (precision != NNGP_FP64 && precision != NNGP_FP32R)
+    return nngp_fail(ctx, NNGP_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32R)");
+  double *xy, *Vrm = nullptr;
+  NNGP_ALLOC(ctx, xy, double, S_COORDS, 2 * (size_t)n);
+  interleave_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d_coords_cm, n, xy);
+  NNGP_LAUNCH_CHECK(ctx);
+  if (mode == 1) {
+    NNGP_ALLOC(ctx, Vrm, double, S_V, (size_t)n * nv);
+    const long tot = (long)n * nv;
+    to_row_major_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(d_V_cm, n, nv, Vrm);
+    NNGP_LAUNCH_CHECK(ctx);
+  }
+  CovParams *d_theta;
+  unsigned long long *d_status;
+  double *d_out;
+  NNGP_ALLOC(ctx, d_theta, CovParams, S_THETA, 1);
+  NNGP_ALLOC(ctx, d_status, unsigned long long, S_STATUS, 1);
+  const int ng = mode == 1 ? 1 + nv * (nv + 1) / 2 : 1;
+  NNGP_ALLOC(ctx, d_out, double, S_RED, 2 * (size_t)ng);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(d_theta, &cp, sizeof cp, cudaMemcpyHostToDevice, ctx->stream));
+  int st = nngp_reset_status(ctx, d_status);
+  if (st) return st;
+  BFData d{};
+  d.n = n;
+  d.m = m;
+  d.nv = nv;
+  d.xy = xy;
+  d.nnIndx = d_nnIndx;
+  d.nnLU = d_nnLU;
+  d.V = Vrm;
+  d.B = d_B;
+  d.F = d_F;
+  BFPlan plan;
+  st = nngp_bf_plan(ctx, &plan, precision, mode, nv, {d}, d_theta, {PassEval{0, 0}}, d_status);
+  if (!st) st = nngp_bf_run(ctx, &plan, d_out);
+  if (!st) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, d_out, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx->stream));
+  nngp_bf_plan_free(ctx, &plan);
+  if (st) return st;
+  return nngp_check_status(ctx, d_status, mode == 0 ? "updateBF" : "loglik_gram");
+}
+
+// Unpacks the upper-triangle (a <= b, row-major) sums into a full nv x nv matrix.
+void unpack_gram(const double *packed, int nv, double *gram) {
+  int k = 0;
+  for (int a = 0; a < nv; a++)
+    for (int b = a; b < nv; b++) {
+      gram[(size_t)b * nv + a] = packed[k];
+      gram[(size_t)a * nv + b] = packed[k];
+      k++;
+    }
+}
+
+struct HostUpload {
+  double *coords = nullptr;
+  int *nnIndx = nullptr, *nnLU = nullptr;
+};
+
+int upload_graph(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                 const int *nnIndxLU, HostUpload &u) {
+  const int64_t nI = nngp_nindx(n, m);
+  NNGP_ALLOC(ctx, u.coords, double, S_COORDS0, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, u.nnIndx, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, u.nnLU, int, S_NNLU, 2 * (size_t)n);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u.coords, coords, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (nI > 0)
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u.nnIndx, nnIndx, sizeof(int) * nI, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u.nnLU, nnIndxLU, sizeof(int) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  return NNGP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nngp_updateBF_dev(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                      const int *nnIndxLU, int covModel, const double *theta, int precision,
+                      double *B, double *F, double *logDet) {
+  int st = check_common(ctx, n, m, covModel);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
+  double ld = 0.0;
+  st = run_single(ctx, 0, n, m, 0, coords, nnIndx, nnIndxLU, nullptr, cp, precision, B, F, &ld);
+  if (st) return st;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(logDet, &ld, sizeof ld, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_loglik_gram_dev(nngp_ctx *ctx, int n, int m, int nv, const double *coords,
+                         const int *nnIndx, const int *nnIndxLU, const double *V, int covModel,
+                         const double *theta, int precision, double *logDet, double *gram) {
+  int st = check_common(ctx, n, m, covModel);
+  if (st) return st;
+  if (nv < 1 || nv > NNGP_MAX_NV) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= nv <= 8 required");
+  cudaSetDevice(ctx->device);
+  const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
+  double packed[1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2];
+  st = run_single(ctx, 1, n, m, nv, coords, nnIndx, nnIndxLU, V, cp, precision, nullptr, nullptr, packed);
+  if (st) return st;
+  double full[NNGP_MAX_NV * NNGP_MAX_NV];
+  unpack_gram(packed + 1, nv, full);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(logDet, packed, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(gram, full, sizeof(double) * nv * nv, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_updateBF(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                  const int *nnIndxLU, int covModel, const double *theta, int precision,
+                  double *B, double *F, double *logDet) {
+  int st = check_common(ctx, n, m, covModel);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  HostUpload u;
+  if ((st = upload_graph(ctx, n, m, coords, nnIndx, nnIndxLU, u))) return st;
+  const int64_t nI = nngp_nindx(n, m);
+  double *dB, *dF;
+  NNGP_ALLOC(ctx, dB, double, S_B, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dF, double, S_F, (size_t)n);
+  const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
+  st = run_single(ctx, 0, n, m, 0, u.coords, u.nnIndx, u.nnLU, nullptr, cp, precision, dB, dF, logDet);
+  if (st) return st;
+  if (nI > 0) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(B, dB, sizeof(double) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(F, dF, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  // location 0 has no neighbors; the reference stores B[0] = 0 before location 1
+  // overwrites that slot, so nothing further is needed here.
+  return NNGP_OK;
+}
+
+int nngp_updateConjBF(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
+                      const int *nnIndxLU, int covModel, double phi, double alpha, double nu,
+                      int precision, double *B, double *F) {
+  const double theta[4] = {1.0, alpha, phi, nu};
+  double ld = 0.0;
+  return nngp_updateBF(ctx, n, m, coords, nnIndx, nnIndxLU, covModel, theta, precision, B, F, &ld);
+}
+
+int nngp_loglik_gram(nngp_ctx *ctx, int n, int m, int nv, const double *coords,
+                     const int *nnIndx, const int *nnIndxLU, const double *V, int covModel,
+                     const double *theta, int precision, double *logDet, double *gram) {
+  int st = check_common(ctx, n, m, covModel);
+  if (st) return st;
+  if (nv < 1 || nv > NNGP_MAX_NV) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= nv <= 8 required");
+  cudaSetDevice(ctx->device);
+  HostUpload u;
+  if ((st = upload_graph(ctx, n, m, coords, nnIndx, nnIndxLU, u))) return st;
+  double *dV;
+  NNGP_ALLOC(ctx, dV, double, S_V2, (size_t)n * nv);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dV, V, sizeof(double) * n * nv, cudaMemcpyHostToDevice, ctx->stream));
+  const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
+  double packed[1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2];
+  st = run_single(ctx, 1, n, m, nv, u.coords, u.nnIndx, u.nnLU, dV, cp, precision, nullptr, nullptr, packed);
+  if (st) return st;
+  *logDet = packed[0];
+  unpack_gram(packed + 1, nv, gram);
+  return NNGP_OK;
+}
+
+int nngp_Q(nngp_ctx *ctx, const double *B, const double *F, const double *u, const double *v,
+           int n, const int *nnIndx, const int *nnIndxLU, double *q) {
+  if (!ctx || n < 1) return nngp_fail(ctx, NNGP_ERR_ARG, "n >= 1 required");
+  cudaSetDevice(ctx->device);
+  // the packed length is the sum of the counts
+  int64_t nI = 0;
+  {
+    // counts are the second half of nnIndxLU; offsets of the last location + its count
+    nI = (int64_t)nnIndxLU[n - 1] + nnIndxLU[2 * n - 1];
+  }
+  double *dB, *dF, *du, *dv, *dpart, *dq;
+  int *dI, *dLU;
+  NNGP_ALLOC(ctx, dB, double, S_B, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dF, double, S_F, (size_t)n);
+  NNGP_ALLOC(ctx, du, double, S_U, (size_t)n);
+  NNGP_ALLOC(ctx, dv, double, S_V2, (size_t)n);
+  NNGP_ALLOC(ctx, dI, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dLU, int, S_NNLU, 2 * (size_t)n);
+  const int nb = (n + 255) / 256;
+  NNGP_ALLOC(ctx, dpart, double, S_PARTIAL, (size_t)nb);
+  NNGP_ALLOC(ctx, dq, double, S_RED, 1);
+  if (nI > 0) {
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dB, B, sizeof(double) * nI, cudaMemcpyHostToDevice, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dI, nnIndx, sizeof(int) * nI, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dF, F, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(du, u, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dv, v, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dLU, nnIndxLU, sizeof(int) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  q_kernel<<<nb, 256, 0, ctx->stream>>>(dB, dF, du, dv, n, dI, dLU, dpart);
+  NNGP_LAUNCH_CHECK(ctx);
+  sum_kernel<<<1, 256, 0, ctx->stream>>>(dpart, nb, dq);
+  NNGP_LAUNCH_CHECK(ctx);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(q, dq, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+}  // extern "C"

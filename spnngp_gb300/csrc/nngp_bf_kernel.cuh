@@ -1,0 +1,385 @@
+// Kernel template of the B/F neighborhood-solve pass (instantiated in
+// nngp_bf_inst_*.cu, dispatched from nngp_bf.cu): one thread solves one location's m x m
+// neighborhood system (reference updateBF, src/rNNGP.cpp:46-101, and
+// updateConjBF, src/cNNGP.cpp:24-69).
+//
+// Layout: a block owns a tile of TPB consecutive locations of one job (job =
+// one dataset at one parameter set).  Each thread keeps the packed lower
+// triangle of its covariance in shared memory, interleaved across threads
+// (element e of thread t at tri[e*TPB + t], so every access is bank-conflict
+// free), and the row being factored plus 1/diag in registers.  The Cholesky is
+// the row-oriented (Banachiewicz) form: row r of L needs only rows < r, one
+// shared load per FMA.  The forward solve for c is fused into the factor loop;
+// B is the back substitution.
+//
+// Precision modes:
+//   FP64   everything in double.
+//   FP32R  coordinates differenced in FP64 and split into float hi/lo parts;
+//          covariance build, Cholesky and both triangular solves in float; then
+//          one refinement step: the residual c - C b is accumulated in FP64 (the
+//          float entries of C and b multiply exactly in double), the correction
+//          is solved with the float factor, and B = b + delta is kept in FP64.
+//          F, log F and the Gram sums are FP64.  A location whose float pivot is
+//          not positive is flagged and re-solved by the FP64 kernel.
+//
+// Modes: 0 writes B (packed, nIndx) and F and per-tile sums of log F;
+//        1 (fused likelihood) writes no B/F but per-tile sums of log F and of
+//        r_a r_b / F for r = (I - B) V at the location, V = [X y].
+// Per-tile sums are reduced in a fixed order, so results do not depend on the
+// launch shape or on block scheduling.
+#pragma once
+#include <cuda_runtime.h>
+#include <type_traits>
+#include "nngp_internal.h"
+#include "nngp_math.cuh"
+
+namespace nngp_bf {
+
+constexpr int kNGMax = 1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2;
+// FP32R hands a location to the FP64 kernel when F < kFp32rMinF * (sigma^2 + tau^2).
+constexpr double kFp32rMinF = 1e-3;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void record_status(unsigned long long *st, unsigned long long code,
+                                              long long loc) {
+  atomicMin(st, (code << 48) | (unsigned long long)(loc & 0xFFFFFFFFFFFFll));
+}
+
+// Finds the job owning `tile` (jobs sorted by tile0).
+__device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].tile0 <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Block-level fixed-order reduction of the per-thread values produced by `val(k)`
+// for k < ng; thread 0.. write out[k].
+template <int TPB, typename F>
+__device__ __forceinline__ void block_reduce_store(int ng, F val, double *wbuf, double *out) {
+  constexpr int W = TPB / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = 0; k < ng; k++) {
+    const double s = warp_sum(val(k));
+    if (lane == 0) wbuf[w * kNGMax + k] = s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < ng; k += TPB) {
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t < W; t++) s += wbuf[t * kNGMax + k];
+    out[k] = s;
+  }
+}
+
+template <int M>
+__host__ __device__ constexpr int tri_size() { return M * (M + 1) / 2; }
+__host__ __device__ constexpr int tri_at(int r, int c) { return r * (r + 1) / 2 + c; }
+
+// --------------------------------------------------------------------- kernel
+template <int M, bool R32, int MODE, int TPB>
+__global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ datas,
+                                                 const CovParams *__restrict__ thetas,
+                                                 const BFJob *__restrict__ jobs, int njobs,
+                                                 int total_tiles, int nv,
+                                                 unsigned long long *__restrict__ status,
+                                                 int only_flagged) {
+  using T = typename std::conditional<R32, float, double>::type;
+  constexpr int TRI = tri_size<M>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *tri = reinterpret_cast<T *>(smem_raw);
+  // per-neighbor geometry: FP32R 4 floats (dx hi, dy hi, dx lo, dy lo) relative to the
+  // location; FP64 2 doubles (absolute x, y)
+  T *geo = tri + (size_t)TRI * TPB;
+  constexpr int GEO = R32 ? 4 : 2;
+  double *wbuf = reinterpret_cast<double *>(geo + (size_t)GEO * M * TPB);
+  const int tid = threadIdx.x;
+#define TRI_(r, c) tri[(size_t)tri_at((r), (c)) * TPB + tid]
+#define GEO_(k, q) geo[(size_t)((k) * GEO + (q)) * TPB + tid]
+
+  for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+    const int jid = find_job(jobs, njobs, tile);
+    const BFJob job = jobs[jid];
+    const BFData d = datas[job.data];
+    const CovParams *cpp = thetas + job.theta;
+    const double sigmaSq = cpp->sigmaSq, tauSq = cpp->tauSq;
+    const int tj = tile - job.tile0;
+    const int i = tj * TPB + tid;
+    bool active = i < d.n;
+    if (active && only_flagged) active = job.flags[i] != 0;
+
+    int mi = 0, off = 0;
+    double xi = 0.0, yi = 0.0;
+    int nb[M];
+    if (active) {
+      off = d.nnLU[i];
+      mi = d.nnLU[d.n + i];
+      const double2 p = reinterpret_cast<const double2 *>(d.xy)[i];
+      xi = p.x;
+      yi = p.y;
+    }
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      nb[k] = 0;
+      if (k < mi) {
+        nb[k] = d.nnIndx[off + k];
+        const double2 q = reinterpret_cast<const double2 *>(d.xy)[nb[k]];
+        if constexpr (R32) {
+          const double ddx = q.x - xi, ddy = q.y - yi;
+          const float hx = (float)ddx, hy = (float)ddy;
+          GEO_(k, 0) = hx;
+          GEO_(k, 1) = hy;
+          GEO_(k, 2) = (float)(ddx - (double)hx);
+          GEO_(k, 3) = (float)(ddy - (double)hy);
+        } else {
+          GEO_(k, 0) = q.x;
+          GEO_(k, 1) = q.y;
+        }
+      }
+    }
+
+    // ---- covariance build: c (registers) and the lower triangle of C (shared)
+    T cv[M];
+    const T s2 = (T)sigmaSq, t2 = (T)tauSq;
+    const float phif = (float)cpp->phi;
+#pragma unroll
+    for (int r = 0; r < M; r++) {
+      cv[r] = (T)0;
+      if (r < mi) {
+        if constexpr (R32) {
+          const float hx = GEO_(r, 0), hy = GEO_(r, 1);
+          cv[r] = s2 * nngp_cor_f(hx * hx + hy * hy, *cpp, phif);
+#pragma unroll
+          for (int c = 0; c <= r; c++) {
+            float e;
+            if (c == r) {
+              e = s2 + t2;  // every model has rho(0) = 1
+            } else {
+              const float ex = (GEO_(r, 0) - GEO_(c, 0)) + (GEO_(r, 2) - GEO_(c, 2));
+              const float ey = (GEO_(r, 1) - GEO_(c, 1)) + (GEO_(r, 3) - GEO_(c, 3));
+              e = s2 * nngp_cor_f(ex * ex + ey * ey, *cpp, phif);
+            }
+            TRI_(r, c) = (T)e;
+          }
+        } else {
+          const double xr = GEO_(r, 0), yr = GEO_(r, 1);
+          const double ax = xi - xr, ay = yi - yr;
+          cv[r] = sigmaSq * nngp_cor_d(sqrt(ax * ax + ay * ay), *cpp);
+#pragma unroll
+          for (int c = 0; c <= r; c++) {
+            const double bx = xr - GEO_(c, 0), by = yr - GEO_(c, 1);
+            double e = sigmaSq * nngp_cor_d(sqrt(bx * bx + by * by), *cpp);
+            if (c == r) e += tauSq;
+            TRI_(r, c) = (T)e;
+          }
+        }
+      }
+    }
+
+    // ---- Cholesky (row-oriented) fused with the forward solve L z = c
+    T invd[M], z[M];
+    bool ok = true;
+#pragma unroll
+    for (int r = 0; r < M; r++) {
+      invd[r] = (T)0;
+      z[r] = (T)0;
+      if (r < mi) {
+        T row[M];
+#pragma unroll
+        for (int c = 0; c <= r; c++) {
+          T s = TRI_(r, c);
+#pragma unroll
+          for (int k = 0; k < c; k++) s -= row[k] * ((c == r) ? row[k] : TRI_(c, k));
+          if (c < r) {
+            row[c] = s * invd[c];
+          } else {
+            ok = ok && (s > (T)0);
+            const T dg = sqrt(s);
+            row[r] = dg;
+            invd[r] = (T)1 / dg;
+          }
+        }
+        T zs = cv[r];
+#pragma unroll
+        for (int k = 0; k < r; k++) zs -= row[k] * z[k];
+        z[r] = zs * invd[r];
+#pragma unroll
+        for (int c = 0; c <= r; c++) TRI_(r, c) = row[c];
+      }
+    }
+
+    // ---- back substitution L' b = z
+    T bb[M];
+#pragma unroll
+    for (int k = M - 1; k >= 0; k--) {
+      bb[k] = (T)0;
+      if (k < mi) {
+        bb[k] = z[k] * invd[k];
+#pragma unroll
+        for (int r = 0; r < k; r++) z[r] -= TRI_(k, r) * bb[k];
+      }
+    }
+
+    double Bd[M];
+    if constexpr (R32) {
+      if (!ok && active) {
+        // float pivot failed: leave this location to the FP64 kernel
+        job.flags[i] = 1;
+        active = false;
+        mi = 0;
+      }
+      // ---- refinement: res = c - C b in FP64 with C rebuilt bit-identically
+      double res[M];
+#pragma unroll
+      for (int r = 0; r < M; r++) res[r] = (r < mi) ? (double)cv[r] : 0.0;
+#pragma unroll
+      for (int r = 0; r < M; r++) {
+        if (r < mi) {
+#pragma unroll
+          for (int c = 0; c <= r; c++) {
+            float e;
+            if (c == r) {
+              e = s2 + t2;
+            } else {
+              const float ex = (GEO_(r, 0) - GEO_(c, 0)) + (GEO_(r, 2) - GEO_(c, 2));
+              const float ey = (GEO_(r, 1) - GEO_(c, 1)) + (GEO_(r, 3) - GEO_(c, 3));
+              e = s2 * nngp_cor_f(ex * ex + ey * ey, *cpp, phif);
+            }
+            const double ed = (double)e;
+            res[r] = fma(-ed, (double)bb[c], res[r]);
+            if (c < r) res[c] = fma(-ed, (double)bb[r], res[c]);
+          }
+        }
+      }
+      // correction: L L' delta = res, in float with the float factor
+      T w[M];
+#pragma unroll
+      for (int r = 0; r < M; r++) {
+        w[r] = (T)0;
+        if (r < mi) {
+          T s = (T)res[r];
+#pragma unroll
+          for (int k = 0; k < r; k++) s -= TRI_(r, k) * w[k];
+          w[r] = s * invd[r];
+        }
+      }
+#pragma unroll
+      for (int k = M - 1; k >= 0; k--) {
+        Bd[k] = 0.0;
+        if (k < mi) {
+          const T dk = w[k] * invd[k];
+#pragma unroll
+          for (int r = 0; r < k; r++) w[r] -= TRI_(k, r) * dk;
+          Bd[k] = (double)bb[k] + (double)dk;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; k++) Bd[k] = (double)bb[k];
+      if (!ok && active) record_status(status, 1, i);
+    }
+
+    // ---- F = sigma^2 + tau^2 - B'c in FP64
+    double Fi = sigmaSq + tauSq;
+    {
+      double dot = 0.0;
+#pragma unroll
+      for (int k = 0; k < M; k++)
+        if (k < mi) dot = fma(Bd[k], (double)cv[k], dot);
+      Fi = sigmaSq - dot + tauSq;
+    }
+    if constexpr (R32) {
+      // a conditional variance this small is dominated by the float rounding of C:
+      // hand the location to the FP64 kernel
+      if (active && !(Fi > kFp32rMinF * (sigmaSq + tauSq))) {
+        job.flags[i] = 1;
+        active = false;
+        mi = 0;
+      }
+    }
+    const double logF = active ? log(Fi) : 0.0;
+
+    if (MODE == 0) {
+      if (active) {
+#pragma unroll
+        for (int k = 0; k < M; k++)
+          if (k < mi) d.B[off + k] = Bd[k];
+        d.F[i] = Fi;
+      }
+      block_reduce_store<TPB>(1, [&](int) { return logF; }, wbuf, job.partial + (size_t)tj * 1);
+    } else {
+      // r_v = V_i,v - sum_k B_k V_N(k),v for the nv columns, then r_a r_b / F
+      double rv[NNGP_MAX_NV];
+#pragma unroll
+      for (int v = 0; v < NNGP_MAX_NV; v++) {
+        rv[v] = 0.0;
+        if (active && v < nv) {
+          double s = d.V[(size_t)i * nv + v];
+#pragma unroll
+          for (int k = 0; k < M; k++)
+            if (k < mi) s = fma(-Bd[k], d.V[(size_t)nb[k] * nv + v], s);
+          rv[v] = s;
+        }
+      }
+      const double invF = active ? 1.0 / Fi : 0.0;
+      const int ng = 1 + nv * (nv + 1) / 2;
+      block_reduce_store<TPB>(
+          ng,
+          [&](int k) -> double {
+            if (k == 0) return logF;
+            // k-1 enumerates (a, b), a <= b, row-major
+            int t = k - 1, a = 0;
+            while (t >= nv - a) { t -= nv - a; a++; }
+            const int b = a + t;
+            double ra = 0.0, rb = 0.0;
+#pragma unroll
+            for (int v = 0; v < NNGP_MAX_NV; v++) {
+              if (v == a) ra = rv[v];
+              if (v == b) rb = rv[v];
+            }
+            return ra * rb * invF;
+          },
+          wbuf, job.partial + (size_t)tj * ng);
+    }
+    __syncthreads();
+  }
+#undef TRI_
+#undef GEO_
+}
+
+template <int M, bool R32>
+constexpr int bf_tpb() {
+  return R32 ? (M <= 16 ? 128 : 64) : (M <= 16 ? 64 : 32);
+}
+
+template <int M, bool R32, int MODE>
+int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass) {
+  constexpr int TPB = bf_tpb<M, R32>();
+  using T = typename std::conditional<R32, float, double>::type;
+  constexpr int GEO = R32 ? 4 : 2;
+  const size_t smem = sizeof(T) * ((size_t)tri_size<M>() + (size_t)GEO * M) * TPB +
+                      sizeof(double) * (TPB / 32) * kNGMax;
+  auto kern = bf_kernel<M, R32, MODE, TPB>;
+  static bool configured = false;  // once per instantiation
+  if (!configured) {
+    NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  const int tiles = fallback_pass ? pl->tiles_fb : pl->tiles;
+  const BFJob *jobs = fallback_pass ? pl->d_jobs_fb : pl->d_jobs;
+  if (tiles <= 0) return NNGP_OK;
+  kern<<<tiles, TPB, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, jobs, pl->njobs, tiles, pl->nv,
+                                          pl->d_status, fallback_pass ? 1 : 0);
+  NNGP_LAUNCH_CHECK(ctx);
+  return NNGP_OK;
+}
+
+}  // namespace nngp_bf

@@ -1,0 +1,380 @@
+// Model drivers other than the MCMC: the conjugate fit + prediction
+// (reference cNNGP, src/cNNGP.cpp:73-358), response prediction (rNNGPPredict,
+// src/rNNGPPredict.cpp:25-223) and replicated data (rNNGPReplicated,
+// src/rNNGPReplicated.cpp:74-244).
+//
+// cNNGP runs all g parameter sets in one fused likelihood pass (g jobs over the
+// same dataset), then one thread per set does the p x p algebra
+// (src/cNNGP.cpp:226-249), then one thread per (set, prediction point) solves
+// the prediction neighborhood.  rNNGPReplicated runs the standalone B/F pass
+// for all kept samples at once and one thread per sample walks the sequential
+// recurrence.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <vector>
+#include "nngp_internal.h"
+#include "nngp_pred.h"
+#include "nngp_small.cuh"
+
+using nngp_pred::KIND_CONJ;
+using nngp_pred::KIND_RESP;
+using nngp_pred::PredArgs;
+
+namespace {
+
+__global__ void interleave_kernel3(const double *__restrict__ cm, int n, double *__restrict__ xy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    xy[2 * i] = cm[i];
+    xy[2 * i + 1] = cm[n + i];
+  }
+}
+
+__global__ void build_v_kernel3(const double *__restrict__ X, const double *__restrict__ y, int n, int p,
+                                double *__restrict__ V) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = p + 1;
+  if (t < (long)n * nv) {
+    const int i = (int)(t / nv), v = (int)(t % nv);
+    V[t] = (v < p) ? X[(size_t)v * n + i] : (y ? y[i] : 0.0);
+  }
+}
+
+// Per parameter set: beta-hat, a*, b*, bB^-1 (lower), bb from the Gram (src/cNNGP.cpp:226-249).
+__global__ void conj_fit_kernel(const double *__restrict__ out, int ng, int g, int p, int n, double aIG,
+                                double bIG, double *__restrict__ betaHat, double *__restrict__ ab,
+                                double *__restrict__ bBInv, double *__restrict__ bb,
+                                unsigned long long *__restrict__ status) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g) return;
+  const int nv = p + 1;
+  const double *o = out + (size_t)k * ng;
+  double G[NNGP_MAX_NV * NNGP_MAX_NV];
+  int t = 1;
+  for (int a = 0; a < nv; a++)
+    for (int b = a; b < nv; b++) {
+      G[b * nv + a] = o[t];
+      G[a * nv + b] = o[t];
+      t++;
+    }
+  double V[(NNGP_MAX_NV - 1) * (NNGP_MAX_NV - 1)], v[NNGP_MAX_NV - 1], bh[NNGP_MAX_NV - 1];
+  for (int i = 0; i < p; i++) {
+    v[i] = G[p * nv + i];
+    for (int j = 0; j < p; j++) V[j * p + i] = (j <= i) ? G[j * nv + i] : 0.0;
+  }
+  if (!small_potrf(V, p)) {
+    atomicMin(status, (2ull << 48) | (unsigned long long)k);
+    return;
+  }
+  small_potri(V, p);
+  small_symv(V, p, v, bh);
+  double bv = 0.0;
+  for (int i = 0; i < p; i++) bv += bh[i] * v[i];
+  ab[2 * k] = aIG + 1.0 * n / 2.0;
+  ab[2 * k + 1] = bIG + 0.5 * (G[p * nv + p] - bv);
+  for (int i = 0; i < p; i++) {
+    betaHat[(size_t)k * p + i] = bh[i];
+    bb[(size_t)k * p + i] = v[i];
+  }
+  for (int i = 0; i < p * p; i++) bBInv[(size_t)k * p * p + i] = V[i];
+}
+
+// v_i = B_i v_N(i) + sqrt(F_i) z_i, then y_rep = v + X beta_s; one thread per sample.
+__global__ void replicate_kernel(int ns, int n, int p, const double *__restrict__ B, int64_t nI,
+                                 const double *__restrict__ F, const int *__restrict__ nnIndx,
+                                 const int *__restrict__ nnLU, const double *__restrict__ z,
+                                 const double *__restrict__ X, const double *__restrict__ beta, int nSamples,
+                                 int s0, double *__restrict__ yRep) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  const int s = s0 + t;
+  const double *Bs = B + (size_t)t * nI;
+  const double *Fs = F + (size_t)t * n;
+  const double *zs = z + (size_t)s * n;
+  double *out = yRep + (size_t)s * n;
+  for (int i = 0; i < n; i++) {
+    const int off = nnLU[i], cnt = nnLU[n + i];
+    double acc = 0.0;
+    for (int j = 0; j < cnt; j++) acc += Bs[off + j] * out[nnIndx[off + j]];
+    out[i] = acc + sqrt(Fs[i]) * zs[i];
+  }
+  for (int i = 0; i < n; i++) {
+    double xb = 0.0;
+    for (int j = 0; j < p; j++) xb += X[(size_t)j * n + i] * beta[s + (size_t)nSamples * j];
+    out[i] += xb;
+  }
+}
+
+inline unsigned nb(long cnt, int tpb) { return (unsigned)((cnt + tpb - 1) / tpb); }
+
+struct Tmp {
+  nngp_ctx *ctx;
+  std::vector<void *> v;
+  bool bad = false;
+  explicit Tmp(nngp_ctx *c) : ctx(c) {}
+  void *up(const void *h, size_t bytes) {
+    void *d = nngp_malloc_async(ctx, bytes ? bytes : 16);
+    if (!d) bad = true;
+    else if (h && bytes) cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    v.push_back(d);
+    return d;
+  }
+  ~Tmp() {
+    for (void *q : v) nngp_free_async(ctx, q);
+    cudaStreamSynchronize(ctx->stream);
+  }
+};
+
+int launch_pred_any(nngp_ctx *ctx, int precision, int kind, const PredArgs &a) {
+  using namespace nngp_pred;
+  const bool r32 = precision == NNGP_FP32R;
+  if (a.m <= 16) {
+    if (kind == KIND_CONJ) return r32 ? launch_pred<16, true, KIND_CONJ>(ctx, a) : launch_pred<16, false, KIND_CONJ>(ctx, a);
+    return r32 ? launch_pred<16, true, KIND_RESP>(ctx, a) : launch_pred<16, false, KIND_RESP>(ctx, a);
+  }
+  if (kind == KIND_CONJ) return r32 ? launch_pred<32, true, KIND_CONJ>(ctx, a) : launch_pred<32, false, KIND_CONJ>(ctx, a);
+  return r32 ? launch_pred<32, true, KIND_RESP>(ctx, a) : launch_pred<32, false, KIND_RESP>(ctx, a);
+}
+
+// Runs the prediction kernel; an FP32R factor failure reruns the whole launch in FP64.
+int run_pred(nngp_ctx *ctx, int precision, int kind, PredArgs a, const char *what) {
+  int st = nngp_reset_status(ctx, a.status);
+  if (!st) st = launch_pred_any(ctx, precision, kind, a);
+  if (st) return st;
+  unsigned long long h = 0;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&h, a.status, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h != NNGP_STATUS_OK && (h >> 48) == 4 && precision == NNGP_FP32R) {
+    if ((st = nngp_reset_status(ctx, a.status))) return st;
+    if ((st = launch_pred_any(ctx, NNGP_FP64, kind, a))) return st;
+  }
+  return nngp_check_status(ctx, a.status, what);
+}
+
+CovParams params(int model, double s2, double t2, double phi, double nu) {
+  CovParams c{};
+  c.model = model;
+  c.sigmaSq = s2;
+  c.tauSq = t2;
+  c.phi = phi;
+  c.nu = nu;
+  cov_prepare(c);
+  return c;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nngp_cNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, const double *coords,
+               const double *thetaAlpha, const int *nnIndx, const int *nnIndxLU, const double *X0,
+               const double *coords0, int n0, const int *nnIndx0, int g, int m, const double *sigmaSqIG,
+               int covModel, int precision, double *betaHat, double *ab, double *bBInv, double *bb,
+               double *y0Hat, double *y0HatVar) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (p < 1 || p > NNGP_MAX_NV - 1) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= p <= 7 required");
+  if (n < 1 || m < 1 || m > NNGP_MAX_M || n < m) return nngp_fail(ctx, NNGP_ERR_ARG, "n >= m and 1 <= m <= 32 required");
+  if (covModel < 0 || covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+  if (g < 1 || n0 < 0) return nngp_fail(ctx, NNGP_ERR_ARG, "g >= 1 and n0 >= 0 required");
+  cudaSetDevice(ctx->device);
+  const int nTheta = covModel == 2 ? 3 : 2, nv = p + 1, ng = 1 + nv * (nv + 1) / 2;
+  const int64_t nI = nngp_nindx(n, m);
+  Tmp T(ctx);
+  const double *dcm = (const double *)T.up(coords, sizeof(double) * 2 * n);
+  const int *dnn = (const int *)T.up(nnIndx, sizeof(int) * (nI > 0 ? nI : 0));
+  const int *dlu = (const int *)T.up(nnIndxLU, sizeof(int) * 2 * n);
+  const double *dX = (const double *)T.up(X, sizeof(double) * (size_t)n * p);
+  const double *dy = (const double *)T.up(y, sizeof(double) * n);
+  double *xy = (double *)T.up(nullptr, sizeof(double) * 2 * n);
+  double *V = (double *)T.up(nullptr, sizeof(double) * (size_t)n * nv);
+  std::vector<CovParams> th(g);
+  for (int k = 0; k < g; k++)
+    th[k] = params(covModel, 1.0, thetaAlpha[k * nTheta + 1], thetaAlpha[k * nTheta],
+                   covModel == 2 ? thetaAlpha[k * nTheta + 2] : 0.0);
+  CovParams *dth = (CovParams *)T.up(th.data(), sizeof(CovParams) * g);
+  double *out = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)g * ng);
+  double *dbeta = (double *)T.up(nullptr, sizeof(double) * (size_t)p * g);
+  double *dab = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)g);
+  double *dV = (double *)T.up(nullptr, sizeof(double) * (size_t)p * p * g);
+  double *dbb = (double *)T.up(nullptr, sizeof(double) * (size_t)p * g);
+  unsigned long long *dst = (unsigned long long *)T.up(nullptr, sizeof(unsigned long long));
+  if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  interleave_kernel3<<<nb(n, 256), 256, 0, ctx->stream>>>(dcm, n, xy);
+  build_v_kernel3<<<nb((long)n * nv, 256), 256, 0, ctx->stream>>>(dX, dy, n, p, V);
+  ctx->launches += 2;
+  int st = nngp_reset_status(ctx, dst);
+  if (st) return st;
+  BFData d{};
+  d.n = n;
+  d.m = m;
+  d.nv = nv;
+  d.xy = xy;
+  d.nnIndx = dnn;
+  d.nnLU = dlu;
+  d.V = V;
+  std::vector<PassEval> ev(g);
+  for (int k = 0; k < g; k++) ev[k] = PassEval{0, k};
+  BFPlan plan;
+  st = nngp_bf_plan(ctx, &plan, precision, 1, nv, {d}, dth, ev, dst);
+  if (!st) st = nngp_bf_run(ctx, &plan, out);
+  if (!st) {
+    conj_fit_kernel<<<nb(g, 64), 64, 0, ctx->stream>>>(out, ng, g, p, n, sigmaSqIG[0], sigmaSqIG[1], dbeta, dab,
+                                                       dV, dbb, dst);
+    ctx->launches++;
+  }
+  nngp_bf_plan_free(ctx, &plan);
+  if (st) return st;
+  if ((st = nngp_check_status(ctx, dst, "cNNGP"))) return st;
+  if (n0 > 0) {
+    PredArgs a{};
+    a.n = n;
+    a.m = m;
+    a.p = p;
+    a.n0 = n0;
+    a.npar = g;
+    a.xy = xy;
+    a.V = V;
+    a.c0 = (const double *)T.up(coords0, sizeof(double) * 2 * n0);
+    a.X0 = (const double *)T.up(X0, sizeof(double) * (size_t)n0 * p);
+    a.nn0 = (const int *)T.up(nnIndx0, sizeof(int) * (size_t)n0 * m);
+    a.par = dth;
+    a.beta = dbeta;
+    a.Vinv = dV;
+    a.ab = dab;
+    a.out0 = (double *)T.up(nullptr, sizeof(double) * (size_t)n0 * g);
+    a.out1 = (double *)T.up(nullptr, sizeof(double) * (size_t)n0 * g);
+    a.status = dst;
+    if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+    if ((st = run_pred(ctx, precision, KIND_CONJ, a, "cNNGP prediction"))) return st;
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(y0Hat, a.out0, sizeof(double) * (size_t)n0 * g, cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(y0HatVar, a.out1, sizeof(double) * (size_t)n0 * g, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(betaHat, dbeta, sizeof(double) * (size_t)p * g, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ab, dab, sizeof(double) * 2 * (size_t)g, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(bBInv, dV, sizeof(double) * (size_t)p * p * g, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(bb, dbb, sizeof(double) * (size_t)p * g, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_rNNGPPredict(nngp_ctx *ctx, const double *X, const double *y, const double *coords, int n, int p,
+                      int m, const double *X0, const double *coords0, int q, const int *nnIndx0,
+                      const double *betaSamples, const double *thetaSamples, int nSamples, int covModel,
+                      const double *z, int precision, double *y0) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (p < 1 || p > NNGP_MAX_NV - 1) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= p <= 7 required");
+  if (n < 1 || m < 1 || m > NNGP_MAX_M || n < m) return nngp_fail(ctx, NNGP_ERR_ARG, "n >= m and 1 <= m <= 32 required");
+  if (covModel < 0 || covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+  if (q < 0 || nSamples < 0) return nngp_fail(ctx, NNGP_ERR_ARG, "q >= 0 and n.samples >= 0 required");
+  if (q == 0 || nSamples == 0) return NNGP_OK;
+  cudaSetDevice(ctx->device);
+  const int nTheta = covModel == 2 ? 4 : 3;
+  Tmp T(ctx);
+  std::vector<CovParams> th(nSamples);
+  for (int s = 0; s < nSamples; s++) {
+    const double *t = thetaSamples + (size_t)s * nTheta;
+    th[s] = params(covModel, t[0], t[1], t[2], covModel == 2 ? t[3] : 0.0);
+  }
+  PredArgs a{};
+  a.n = n;
+  a.m = m;
+  a.p = p;
+  a.n0 = q;
+  a.npar = nSamples;
+  const double *dcm = (const double *)T.up(coords, sizeof(double) * 2 * n);
+  const double *dX = (const double *)T.up(X, sizeof(double) * (size_t)n * p);
+  const double *dy = (const double *)T.up(y, sizeof(double) * n);
+  double *xy = (double *)T.up(nullptr, sizeof(double) * 2 * n);
+  double *V = (double *)T.up(nullptr, sizeof(double) * (size_t)n * (p + 1));
+  a.c0 = (const double *)T.up(coords0, sizeof(double) * 2 * q);
+  a.X0 = (const double *)T.up(X0, sizeof(double) * (size_t)q * p);
+  a.nn0 = (const int *)T.up(nnIndx0, sizeof(int) * (size_t)q * m);
+  a.par = (const CovParams *)T.up(th.data(), sizeof(CovParams) * nSamples);
+  a.beta = (const double *)T.up(betaSamples, sizeof(double) * (size_t)p * nSamples);
+  a.z = (const double *)T.up(z, sizeof(double) * (size_t)q * nSamples);
+  a.out0 = (double *)T.up(nullptr, sizeof(double) * (size_t)q * nSamples);
+  a.status = (unsigned long long *)T.up(nullptr, sizeof(unsigned long long));
+  if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  interleave_kernel3<<<nb(n, 256), 256, 0, ctx->stream>>>(dcm, n, xy);
+  build_v_kernel3<<<nb((long)n * (p + 1), 256), 256, 0, ctx->stream>>>(dX, dy, n, p, V);
+  ctx->launches += 2;
+  a.xy = xy;
+  a.V = V;
+  int st = run_pred(ctx, precision, KIND_RESP, a, "rNNGPPredict");
+  if (st) return st;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(y0, a.out0, sizeof(double) * (size_t)q * nSamples, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, const double *coords,
+                         int covModel, const int *nnIndx, const int *nnIndxLU, const double *beta,
+                         const double *theta, int nSamples, const double *normals, int precision,
+                         double *yRep) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (p < 1 || n < 1 || m < 1 || m > NNGP_MAX_M || n < m) return nngp_fail(ctx, NNGP_ERR_ARG, "invalid sizes");
+  if (covModel < 0 || covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+  if (nSamples <= 0) return NNGP_OK;
+  cudaSetDevice(ctx->device);
+  const int nTheta = covModel == 2 ? 4 : 3;
+  const int64_t nI = nngp_nindx(n, m);
+  Tmp T(ctx);
+  const double *dcm = (const double *)T.up(coords, sizeof(double) * 2 * n);
+  const int *dnn = (const int *)T.up(nnIndx, sizeof(int) * (nI > 0 ? nI : 0));
+  const int *dlu = (const int *)T.up(nnIndxLU, sizeof(int) * 2 * n);
+  const double *dX = (const double *)T.up(X, sizeof(double) * (size_t)n * p);
+  const double *dbeta = (const double *)T.up(beta, sizeof(double) * (size_t)nSamples * p);
+  const double *dz = (const double *)T.up(normals, sizeof(double) * (size_t)n * nSamples);
+  double *dy = (double *)T.up(nullptr, sizeof(double) * (size_t)n * nSamples);
+  double *xy = (double *)T.up(nullptr, sizeof(double) * 2 * n);
+  std::vector<CovParams> th(nSamples);
+  for (int s = 0; s < nSamples; s++) {
+    const double *t = theta + (size_t)s * nTheta;
+    th[s] = params(covModel, t[0], t[1], t[2], covModel == 2 ? t[3] : 0.0);
+  }
+  CovParams *dth = (CovParams *)T.up(th.data(), sizeof(CovParams) * nSamples);
+  unsigned long long *dst = (unsigned long long *)T.up(nullptr, sizeof(unsigned long long));
+  // samples per chunk: keep the chunk's B arrays near 2 GB
+  const size_t perB = sizeof(double) * (size_t)((nI > 0 ? nI : 1) + n);
+  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nSamples, ((size_t)2 << 30) / perB));
+  double *dB = (double *)T.up(nullptr, sizeof(double) * (size_t)(nI > 0 ? nI : 1) * chunk);
+  double *dF = (double *)T.up(nullptr, sizeof(double) * (size_t)n * chunk);
+  double *out = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)chunk);
+  if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  interleave_kernel3<<<nb(n, 256), 256, 0, ctx->stream>>>(dcm, n, xy);
+  ctx->launches++;
+  int st = nngp_reset_status(ctx, dst);
+  for (int s0 = 0; !st && s0 < nSamples; s0 += chunk) {
+    const int ns = std::min(chunk, nSamples - s0);
+    std::vector<BFData> datas(ns);
+    std::vector<PassEval> ev(ns);
+    for (int t = 0; t < ns; t++) {
+      BFData d{};
+      d.n = n;
+      d.m = m;
+      d.xy = xy;
+      d.nnIndx = dnn;
+      d.nnLU = dlu;
+      d.B = dB + (size_t)t * (nI > 0 ? nI : 1);
+      d.F = dF + (size_t)t * n;
+      datas[t] = d;
+      ev[t] = PassEval{t, s0 + t};
+    }
+    BFPlan plan;
+    st = nngp_bf_plan(ctx, &plan, precision, 0, 0, datas, dth, ev, dst);
+    if (!st) st = nngp_bf_run(ctx, &plan, out);
+    if (!st) {
+      replicate_kernel<<<nb(ns, 32), 32, 0, ctx->stream>>>(ns, n, p, dB, nI > 0 ? nI : 1, dF, dnn, dlu, dz, dX,
+                                                            dbeta, nSamples, s0, dy);
+      ctx->launches++;
+    }
+    nngp_bf_plan_free(ctx, &plan);
+  }
+  if (st) return st;
+  if ((st = nngp_check_status(ctx, dst, "rNNGPReplicated"))) return st;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(yRep, dy, sizeof(double) * (size_t)n * nSamples, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+// Internal host-side structures of the spnngp_gb300 library: the context
+// (device, stream, error state, launch counter) and grow-only device scratch
+// buffers.  Included by every translation unit of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/spnngp_gb300.h"
+
+// Largest neighbor count the dense kernels handle (registers / shared memory are
+// sized from it at compile time).
+constexpr int NNGP_MAX_M = 32;
+// Largest neighbor count of the neighbor-search kernels (lists live in local memory).
+constexpr int NNGP_MAX_M_SEARCH = 64;
+// Largest number of columns of V = [X y] in the fused likelihood pass.
+constexpr int NNGP_MAX_NV = 8;
+
+// Named scratch slots; each is a grow-only device allocation owned by the context.
+enum ScratchSlot {
+  S_COORDS = 0, S_NNINDX, S_NNLU, S_B, S_F, S_V, S_PARTIAL, S_RED, S_THETA, S_STATUS,
+  S_U, S_V2, S_IDX, S_IDX2, S_SORT_TMP, S_XS, S_YS, S_OS, S_NNDIST, S_COORDS0,
+  S_NNINDX0, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4, S_OUT5, S_STREAM_N, S_STREAM_U,
+  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_NUM_SLOTS
+};
+
+struct nngp_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t err_loc = -1;
+  int64_t launches = 0;
+  void *scratch[S_NUM_SLOTS] = {};
+  size_t scratch_cap[S_NUM_SLOTS] = {};
+  // pinned host staging for small results
+  void *pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+
+// Records an error on the context and returns the status.
+int nngp_fail(nngp_ctx *ctx, int status, const std::string &msg, int64_t loc = -1);
+
+// Returns a device buffer of at least `bytes` for `slot` (grows, never shrinks).
+void *nngp_scratch(nngp_ctx *ctx, int slot, size_t bytes);
+void *nngp_pinned(nngp_ctx *ctx, size_t bytes);
+
+#define NNGP_CUDA_TRY(ctx, expr)                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return nngp_fail((ctx), NNGP_ERR_CUDA, std::string(#expr ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define NNGP_LAUNCH_CHECK(ctx)                                                          \
+  do {                                                                                  \
+    (ctx)->launches++;                                                                  \
+    cudaError_t e_ = cudaGetLastError();                                                \
+    if (e_ != cudaSuccess)                                                              \
+      return nngp_fail((ctx), NNGP_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define NNGP_ALLOC(ctx, ptr, type, slot, count)                                          \
+  do {                                                                                  \
+    (ptr) = (type *)nngp_scratch((ctx), (slot), sizeof(type) * (size_t)(count));        \
+    if (!(ptr)) return nngp_fail((ctx), NNGP_ERR_NO_MEMORY, "device allocation failed"); \
+  } while (0)
+
+inline int64_t nngp_nindx(int n, int m) {
+  // (1+m)/2*m + (n-m-1)*m, evaluated as the reference does (src/rNNGP.cpp:218)
+  return (int64_t)((double)(1 + m) / 2 * m + (double)((int64_t)(n - m - 1) * m));
+}
+
+// ------------------------------------------------------------ covariance params
+// One parameter set of the correlation model, prepared on the host (or on the
+// device by the MCMC kernels): model 0 exponential, 1 spherical, 2 matern,
+// 3 gaussian.  For matern, mconst = 1 / (2^(nu-1) Gamma(nu)); when nu = k + 1/2
+// with k <= 8 the closed form exp(-x) * sum_j poly[j] x^j is used (halfk = k),
+// otherwise halfk = -1 and K_nu is evaluated by series / continued fraction.
+struct CovParams {
+  double sigmaSq, tauSq, phi, nu, mconst;
+  double poly[9];
+  int model;
+  int halfk;
+};
+
+// Fills mconst / halfk / poly from model and nu.  Callable on host and device.
+__host__ __device__ inline void cov_prepare(CovParams &c) {
+  c.halfk = -1;
+  c.mconst = 0.0;
+  for (int j = 0; j < 9; j++) c.poly[j] = 0.0;
+  if (c.model != 2) return;
+  c.mconst = 1.0 / (pow(2.0, c.nu - 1.0) * tgamma(c.nu));
+  const double k = c.nu - 0.5;
+  if (k >= 0.0 && k <= 8.0 && k == floor(k)) {
+    const int K = (int)k;
+    c.halfk = K;
+    // rho(x) = exp(-x) * K!/(2K)! * sum_{j=0}^{K} (K+j)!/(j!(K-j)!) (2x)^(K-j)
+    double fact[18];
+    fact[0] = 1.0;
+    for (int t = 1; t < 18; t++) fact[t] = fact[t - 1] * t;
+    const double lead = fact[K] / fact[2 * K];
+    for (int j = 0; j <= K; j++) {
+      const int pw = K - j;
+      c.poly[pw] = lead * fact[K + j] / (fact[j] * fact[K - j]) * ldexp(1.0, pw);
+    }
+  }
+}
+
+// ------------------------------------------------------------- fused-pass jobs
+// One dataset as the dense kernels see it (all device pointers).
+struct BFData {
+  int n, m, nv;
+  const double *xy;      // n x 2 interleaved (x, y)
+  const int *nnIndx;     // packed neighbor lists
+  const int *nnLU;       // [offsets | counts], 2n
+  const double *V;       // n x nv row-major, fused pass only
+  double *B;             // nIndx, standalone pass only
+  double *F;             // n, standalone pass only
+};
+// One (dataset, parameter set) evaluation, covering tiles [tile0, tile0 + ntiles).
+struct BFJob {
+  int data;
+  int theta;
+  int tile0;
+  int ntiles;
+  double *partial;       // ntiles x NG per-tile partial sums
+  unsigned char *flags;  // n bytes: locations the FP32R kernel hands to the FP64 kernel
+};
+
+// A prepared B/F pass over a set of (dataset, parameter set) evaluations.  The
+// job tables live on the device, so nngp_bf_run only launches kernels (it can be
+// captured into a CUDA graph).  Parameter sets are read from device memory at
+// run time, so callers may rewrite them between runs.
+struct BFPlan {
+  int precision = 0, mode = 0, mmax = 0, nv = 0, ng = 0;
+  int njobs = 0, tiles = 0, tiles_fb = 0;
+  BFData *d_datas = nullptr;
+  const CovParams *d_thetas = nullptr;
+  BFJob *d_jobs = nullptr, *d_jobs_fb = nullptr;
+  double *d_partial = nullptr, *d_partial_fb = nullptr;
+  unsigned char *d_flags = nullptr;
+  size_t flags_bytes = 0;
+  unsigned long long *d_status = nullptr;
+  std::vector<void *> owned;
+};
+struct PassEval {
+  int data;
+  int theta;
+};
+// Builds a plan (device allocations owned by the plan, stream-ordered).
+int nngp_bf_plan(nngp_ctx *ctx, BFPlan *plan, int precision, int mode, int nv,
+                 const std::vector<BFData> &datas, const CovParams *d_thetas,
+                 const std::vector<PassEval> &evals, unsigned long long *d_status);
+// Launches the pass; d_out receives njobs x ng sums (log F first, then the Gram
+// entries r_a r_b / F over a <= b, row-major).
+int nngp_bf_run(nngp_ctx *ctx, const BFPlan *plan, double *d_out);
+void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *plan);
+// Stream-ordered device allocation (pooled), freed with nngp_free_async.
+void *nngp_malloc_async(nngp_ctx *ctx, size_t bytes);
+void nngp_free_async(nngp_ctx *ctx, void *p);
+
+// Device status word: 0xFFFF..FF = ok, otherwise (code << 48) | location.
+constexpr unsigned long long NNGP_STATUS_OK = ~0ull;
+int nngp_check_status(nngp_ctx *ctx, unsigned long long *d_status, const char *what);
+int nngp_reset_status(nngp_ctx *ctx, unsigned long long *d_status);

@@ -1,0 +1,543 @@
+// Neighbor search on the GPU.
+//
+// mkNNIndxCB (reference src/nn.cpp:128-258): the mean-distance-ordered search of
+// Ra & Kim (1993).  Locations are sorted by u = x + y; each location walks the
+// sorted order alternately down and up from its own position, stops a direction
+// once ((x_q + y_q) - x_j - y_j)^2 > 2*worst, and accepts predecessors (original
+// index below its own) whose squared distance is strictly below the current
+// worst, re-sorting its m-list with R's Shell sort.  One thread runs one
+// location's walk; distances use __dadd_rn/__dmul_rn so no FMA contraction
+// changes a bit, which makes neighbor indices and distances bit-exact with the
+// reference, ties included.  The sort of u is a radix sort; when two u values
+// are equal the sorted order would depend on R's Shell sort, so in that case the
+// exact Shell-sort passes are replayed on the device instead (each gap's chains
+// are independent insertion sorts, one thread per chain).
+//
+// mkNNIndx (src/nn.cpp:63-111): exhaustive scan j = 0..i-1 per location with
+// the reference's acceptance rule on the Euclidean distance.
+//
+// nn2 (the RANN::nn2 calls of R/spConjNNGP.R:158,311, R/generics.R:642):
+// unconstrained exact kNN of prediction points against the u-sorted training
+// points with the same pruning bound, ordered by (squared distance, index).
+//
+// mkUIndx (src/nn.cpp:25-56, src/util.cpp:115-185): a stable radix sort of the
+// packed neighbor entries by neighbor id gives, for each location, the
+// locations listing it in increasing order, and the entry positions give uiIndx.
+#include <cuda_runtime.h>
+#include <cub/cub.cuh>
+#include <cmath>
+#include <vector>
+#include "nngp_internal.h"
+
+namespace {
+
+__device__ __forceinline__ bool gt_nan_last(double a, double b) {
+  const bool na = isnan(a), nb = isnan(b);
+  if (na && nb) return false;
+  if (na) return true;
+  if (nb) return false;
+  return a > b;
+}
+
+// R's rsort_with_index: Shell sort, Knuth gaps starting above n/9, NaN last.
+__device__ void shell_sort_idx(double *x, int *idx, int n) {
+  int gap = 1;
+  while (gap <= n / 9) gap = 3 * gap + 1;
+  for (; gap > 0; gap /= 3) {
+    for (int i = gap; i < n; i++) {
+      const double key = x[i];
+      const int tag = idx[i];
+      int j = i;
+      while (j >= gap && gt_nan_last(x[j - gap], key)) {
+        x[j] = x[j - gap];
+        idx[j] = idx[j - gap];
+        j -= gap;
+      }
+      x[j] = key;
+      idx[j] = tag;
+    }
+  }
+}
+
+// Packed-list offset / length of location i (src/util.cpp:55-70).
+__device__ __forceinline__ void nn_slot(int i, int m, int &off, int &cnt) {
+  if (i == 0) {
+    off = 0;
+    cnt = 0;
+  } else if (i < m) {
+    off = (int)((double)i / 2 * (i - 1));
+    cnt = i;
+  } else {
+    off = (int)((double)m / 2 * (m - 1) + (double)((i - m) * m));
+    cnt = m;
+  }
+}
+
+__global__ void ukey_kernel(const double *__restrict__ cm, int n, double *__restrict__ u, int *__restrict__ idx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    u[i] = __dadd_rn(cm[i], cm[n + i]);
+    idx[i] = i;
+  }
+}
+
+__global__ void tie_kernel(const double *__restrict__ us, int n, int *__restrict__ flag) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    const double a = us[k];
+    if (a != a || (k + 1 < n && a == us[k + 1])) atomicOr(flag, 1);
+  }
+}
+
+// One gap pass of the Shell sort: thread c owns the chain c, c+h, c+2h, ...
+__global__ void shell_pass_kernel(double *__restrict__ u, int *__restrict__ idx, int n, int h) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= h) return;
+  for (int i = c + h; i < n; i += h) {
+    const double key = u[i];
+    const int tag = idx[i];
+    int j = i;
+    while (j >= h && gt_nan_last(u[j - h], key)) {
+      u[j] = u[j - h];
+      idx[j] = idx[j - h];
+      j -= h;
+    }
+    u[j] = key;
+    idx[j] = tag;
+  }
+}
+
+__global__ void gather_sorted_kernel(const double *__restrict__ cm, int n, const int *__restrict__ sidx,
+                                     double *__restrict__ xs, double *__restrict__ ys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) {
+    const int j = sidx[s];
+    xs[s] = cm[j];
+    ys[s] = cm[n + j];
+  }
+}
+
+// Code-book search for the location at sorted position s.
+__global__ void __launch_bounds__(128) cb_kernel(int n, int m, const double *__restrict__ xs,
+                                                 const double *__restrict__ ys, const int *__restrict__ os,
+                                                 int *__restrict__ nnIndx, double *__restrict__ nnDist,
+                                                 int *__restrict__ nnLU) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const int q = os[s];
+  int off, cnt;
+  nn_slot(q, m, off, cnt);
+  nnLU[q] = off;
+  nnLU[n + q] = cnt;
+  if (cnt == 0) return;
+  double dl[NNGP_MAX_M_SEARCH];
+  int il[NNGP_MAX_M_SEARCH];
+  for (int k = 0; k < cnt; k++) {
+    dl[k] = __longlong_as_double(0x7ff0000000000000ll);
+    il[k] = 0;
+  }
+  double worst = dl[0];
+  const double qx = xs[s], qy = ys[s];
+  const double qu = __dadd_rn(qx, qy);
+  int lo = s, hi = s;
+  bool down = true, up = true;
+  while (down || up) {
+    if (lo == 0) down = false;
+    if (hi == n - 1) up = false;
+    if (down) {
+      lo--;
+      const double cx = xs[lo], cy = ys[lo];
+      const double du = __dadd_rn(__dadd_rn(qu, -cx), -cy);
+      const double dm = __dmul_rn(du, du);
+      if (dm > 2.0 * worst) {
+        down = false;
+      } else {
+        const int j = os[lo];
+        if (j < q) {
+          const double dx = __dadd_rn(qx, -cx), dy = __dadd_rn(qy, -cy);
+          const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+          if (de < worst) {
+            dl[cnt - 1] = de;
+            il[cnt - 1] = j;
+            shell_sort_idx(dl, il, cnt);
+            worst = dl[cnt - 1];
+          }
+        }
+      }
+    }
+    if (up) {
+      hi++;
+      const double cx = xs[hi], cy = ys[hi];
+      const double du = __dadd_rn(__dadd_rn(qu, -cx), -cy);
+      const double dm = __dmul_rn(du, du);
+      if (dm > 2.0 * worst) {
+        up = false;
+      } else {
+        const int j = os[hi];
+        if (j < q) {
+          const double dx = __dadd_rn(qx, -cx), dy = __dadd_rn(qy, -cy);
+          const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+          if (de < worst) {
+            dl[cnt - 1] = de;
+            il[cnt - 1] = j;
+            shell_sort_idx(dl, il, cnt);
+            worst = dl[cnt - 1];
+          }
+        }
+      }
+    }
+  }
+  for (int k = 0; k < cnt; k++) {
+    nnIndx[off + k] = il[k];
+    nnDist[off + k] = __dsqrt_rn(dl[k]);
+  }
+}
+
+// Exhaustive ordered search, location i scans j = 0..i-1 on the Euclidean distance.
+__global__ void __launch_bounds__(128) brute_kernel(int n, int m, const double *__restrict__ cm,
+                                                    int *__restrict__ nnIndx, double *__restrict__ nnDist,
+                                                    int *__restrict__ nnLU) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int off, cnt;
+  nn_slot(i, m, off, cnt);
+  nnLU[i] = off;
+  nnLU[n + i] = cnt;
+  if (cnt == 0) return;
+  double dl[NNGP_MAX_M_SEARCH];
+  int il[NNGP_MAX_M_SEARCH];
+  for (int k = 0; k < cnt; k++) {
+    dl[k] = __longlong_as_double(0x7ff0000000000000ll);
+    il[k] = 0;
+  }
+  double worst = dl[0];
+  double thr = worst;  // squared distances above thr cannot beat worst
+  const double xi = cm[i], yi = cm[n + i];
+  for (int j = 0; j < i; j++) {
+    const double dx = __dadd_rn(xi, -cm[j]), dy = __dadd_rn(yi, -cm[n + j]);
+    const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    if (de > thr) continue;
+    const double d = __dsqrt_rn(de);
+    if (d < worst) {
+      dl[cnt - 1] = d;
+      il[cnt - 1] = j;
+      shell_sort_idx(dl, il, cnt);
+      worst = dl[cnt - 1];
+      thr = worst * worst * (1.0 + 1e-12);
+    }
+  }
+  for (int k = 0; k < cnt; k++) {
+    nnIndx[off + k] = il[k];
+    nnDist[off + k] = dl[k];
+  }
+}
+
+// Exact kNN of one prediction point against the u-sorted training points.
+__global__ void __launch_bounds__(128) nn2_kernel(int n, const double *__restrict__ xs,
+                                                  const double *__restrict__ ys, const int *__restrict__ os,
+                                                  const double *__restrict__ us, int n0,
+                                                  const double *__restrict__ c0, int k,
+                                                  int *__restrict__ outIdx, double *__restrict__ outDist) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n0) return;
+  const double qx = c0[q], qy = c0[n0 + q];
+  const double qu = __dadd_rn(qx, qy);
+  // first sorted position with u >= qu
+  int a = 0, b = n;
+  while (a < b) {
+    const int mid = (a + b) >> 1;
+    if (us[mid] < qu) a = mid + 1;
+    else b = mid;
+  }
+  double dl[NNGP_MAX_M_SEARCH];
+  int il[NNGP_MAX_M_SEARCH];
+  int filled = 0;
+  const double INF = __longlong_as_double(0x7ff0000000000000ll);
+  double worst = INF;
+  int lo = a - 1, hi = a;
+  bool down = lo >= 0, up = hi < n;
+  auto consider = [&](int s) -> bool {  // returns false when the direction is exhausted
+    const double cx = xs[s], cy = ys[s];
+    const double du = __dadd_rn(__dadd_rn(qu, -cx), -cy);
+    const double dm = __dmul_rn(du, du);
+    if (filled == k && dm > 2.0 * worst * (1.0 + 1e-12)) return false;
+    const double dx = __dadd_rn(qx, -cx), dy = __dadd_rn(qy, -cy);
+    const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    const int j = os[s];
+    if (filled == k && !(de < dl[k - 1] || (de == dl[k - 1] && j < il[k - 1]))) return true;
+    int pos = (filled < k) ? filled++ : k - 1;
+    while (pos > 0 && (dl[pos - 1] > de || (dl[pos - 1] == de && il[pos - 1] > j))) {
+      dl[pos] = dl[pos - 1];
+      il[pos] = il[pos - 1];
+      pos--;
+    }
+    dl[pos] = de;
+    il[pos] = j;
+    worst = (filled == k) ? dl[k - 1] : INF;
+    return true;
+  };
+  while (down || up) {
+    if (down) {
+      if (!consider(lo)) down = false;
+      else if (--lo < 0) down = false;
+    }
+    if (up) {
+      if (!consider(hi)) up = false;
+      else if (++hi >= n) up = false;
+    }
+  }
+  for (int t = 0; t < k; t++) {
+    outIdx[(size_t)t * n0 + q] = il[t];
+    if (outDist) outDist[(size_t)t * n0 + q] = __dsqrt_rn(dl[t]);
+  }
+}
+
+__global__ void entry_row_kernel(int n, const int *__restrict__ nnLU, int *__restrict__ erow) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int off = nnLU[r], cnt = nnLU[n + r];
+  for (int k = 0; k < cnt; k++) erow[off + k] = r;
+}
+
+__global__ void iota_kernel(int *__restrict__ a, long cnt) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) a[t] = (int)t;
+}
+
+__global__ void count_kernel(const int *__restrict__ keys, long cnt, int *__restrict__ counts) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) atomicAdd(&counts[keys[t]], 1);
+}
+
+__global__ void uindx_fill_kernel(long cnt, const int *__restrict__ sortedEntry, const int *__restrict__ erow,
+                                  const int *__restrict__ nnLU, int *__restrict__ uIndx, int *__restrict__ uiIndx) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < cnt) {
+    const int e = sortedEntry[t];
+    const int r = erow[e];
+    uIndx[t] = r;
+    uiIndx[t] = e - nnLU[r];
+  }
+}
+
+__global__ void reverse_segments_kernel(int n, const int *__restrict__ ulu, int *__restrict__ uIndx,
+                                        int *__restrict__ uiIndx) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int a = ulu[c], b = ulu[c] + ulu[n + c] - 1;
+  while (a < b) {
+    int t = uIndx[a];
+    uIndx[a] = uIndx[b];
+    uIndx[b] = t;
+    t = uiIndx[a];
+    uiIndx[a] = uiIndx[b];
+    uiIndx[b] = t;
+    a++;
+    b--;
+  }
+}
+
+inline unsigned blocks(long cnt, int tpb) { return (unsigned)((cnt + tpb - 1) / tpb); }
+
+// Sorts (u, index) and builds the sorted SoA view.  coords: device, column-major.
+int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **ys, int **os,
+                double **us, bool exact_ties) {
+  double *u, *u2;
+  int *idx, *idx2;
+  NNGP_ALLOC(ctx, u, double, S_U, (size_t)n);
+  NNGP_ALLOC(ctx, u2, double, S_V2, (size_t)n);
+  NNGP_ALLOC(ctx, idx, int, S_IDX, (size_t)n);
+  NNGP_ALLOC(ctx, idx2, int, S_IDX2, (size_t)n);
+  ukey_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(d_cm, n, u, idx);
+  NNGP_LAUNCH_CHECK(ctx);
+  size_t tmp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp, u, u2, idx, idx2, n, 0, 64, ctx->stream);
+  void *dtmp;
+  NNGP_ALLOC(ctx, dtmp, unsigned char, S_SORT_TMP, tmp);
+  NNGP_CUDA_TRY(ctx, cub::DeviceRadixSort::SortPairs(dtmp, tmp, u, u2, idx, idx2, n, 0, 64, ctx->stream));
+  ctx->launches += 1;
+  if (exact_ties) {
+    int *flag;
+    NNGP_ALLOC(ctx, flag, int, S_MISC, 1);
+    NNGP_CUDA_TRY(ctx, cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+    tie_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(u2, n, flag);
+    NNGP_LAUNCH_CHECK(ctx);
+    int h_flag = 0;
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_flag) {
+      // equal keys: replay R's Shell sort exactly on the unsorted (u, index) pairs
+      std::vector<int> gaps;
+      int gap = 1;
+      while (gap <= n / 9) gap = 3 * gap + 1;
+      for (; gap > 0; gap /= 3) gaps.push_back(gap);
+      for (int h : gaps) {
+        shell_pass_kernel<<<blocks(h, 128), 128, 0, ctx->stream>>>(u, idx, n, h);
+        NNGP_LAUNCH_CHECK(ctx);
+      }
+      NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u2, u, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+      NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(idx2, idx, sizeof(int) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+  }
+  NNGP_ALLOC(ctx, *xs, double, S_XS, (size_t)n);
+  NNGP_ALLOC(ctx, *ys, double, S_YS, (size_t)n);
+  gather_sorted_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(d_cm, n, idx2, *xs, *ys);
+  NNGP_LAUNCH_CHECK(ctx);
+  *os = idx2;
+  if (us) *us = u2;
+  return NNGP_OK;
+}
+
+int check_nn_args(nngp_ctx *ctx, int n, int m) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (n < 1 || m < 1 || m > NNGP_MAX_M_SEARCH)
+    return nngp_fail(ctx, NNGP_ERR_ARG, "n >= 1 and 1 <= m <= 64 required");
+  if (nngp_nindx(n, m) < 0) return nngp_fail(ctx, NNGP_ERR_ARG, "n must be at least m");
+  return NNGP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
+                        double *nnDist, int *nnIndxLU) {
+  int st = check_nn_args(ctx, n, m);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  double *xs, *ys;
+  int *os;
+  if ((st = sorted_view(ctx, n, coords, &xs, &ys, &os, nullptr, true))) return st;
+  cb_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, xs, ys, os, nnIndx, nnDist, nnIndxLU);
+  NNGP_LAUNCH_CHECK(ctx);
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_mkNNIndxCB(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
+                    double *nnDist, int *nnIndxLU) {
+  int st = check_nn_args(ctx, n, m);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  const int64_t nI = nngp_nindx(n, m);
+  double *cm, *dd;
+  int *di, *dlu;
+  NNGP_ALLOC(ctx, cm, double, S_COORDS0, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, di, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dd, double, S_NNDIST, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dlu, int, S_NNLU, 2 * (size_t)n);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(cm, coords, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  if ((st = nngp_mkNNIndxCB_dev(ctx, n, m, cm, di, dd, dlu))) return st;
+  if (nI > 0) {
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnIndx, di, sizeof(int) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnDist, dd, sizeof(double) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnIndxLU, dlu, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_mkNNIndx(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
+                  double *nnDist, int *nnIndxLU) {
+  int st = check_nn_args(ctx, n, m);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  const int64_t nI = nngp_nindx(n, m);
+  double *cm, *dd;
+  int *di, *dlu;
+  NNGP_ALLOC(ctx, cm, double, S_COORDS0, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, di, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dd, double, S_NNDIST, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dlu, int, S_NNLU, 2 * (size_t)n);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(cm, coords, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  brute_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, cm, di, dd, dlu);
+  NNGP_LAUNCH_CHECK(ctx);
+  if (nI > 0) {
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnIndx, di, sizeof(int) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnDist, dd, sizeof(double) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnIndxLU, dlu, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_nn2(nngp_ctx *ctx, int n, const double *coords, int n0, const double *coords0, int k,
+             int *nnIdx, double *nnDist) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (n < 1 || n0 < 0 || k < 1 || k > NNGP_MAX_M_SEARCH || k > n)
+    return nngp_fail(ctx, NNGP_ERR_ARG, "nn2 needs 1 <= k <= min(n, 64)");
+  if (n0 == 0) return NNGP_OK;
+  cudaSetDevice(ctx->device);
+  double *cm, *c0, *dd;
+  int *di;
+  NNGP_ALLOC(ctx, cm, double, S_COORDS0, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, c0, double, S_COORDS, 2 * (size_t)n0);
+  NNGP_ALLOC(ctx, di, int, S_NNINDX0, (size_t)n0 * k);
+  NNGP_ALLOC(ctx, dd, double, S_OUT0, (size_t)n0 * k);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(cm, coords, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(c0, coords0, sizeof(double) * 2 * n0, cudaMemcpyHostToDevice, ctx->stream));
+  double *xs, *ys, *us;
+  int *os;
+  int st = sorted_view(ctx, n, cm, &xs, &ys, &os, &us, false);
+  if (st) return st;
+  nn2_kernel<<<blocks(n0, 128), 128, 0, ctx->stream>>>(n, xs, ys, os, us, n0, c0, k, di, dd);
+  NNGP_LAUNCH_CHECK(ctx);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnIdx, di, sizeof(int) * n0 * k, cudaMemcpyDeviceToHost, ctx->stream));
+  if (nnDist)
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnDist, dd, sizeof(double) * n0 * k, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+int nngp_mkUIndx(nngp_ctx *ctx, int n, int m, const int *nnIndx, int *uIndx, int *uIndxLU,
+                 int *uiIndx, const int *nnIndxLU, int searchType) {
+  int st = check_nn_args(ctx, n, m);
+  if (st) return st;
+  cudaSetDevice(ctx->device);
+  const long nI = (long)nngp_nindx(n, m);
+  int *keys, *keys2, *ent, *ent2, *erow, *dlu, *ulu, *du, *dui;
+  NNGP_ALLOC(ctx, keys, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, keys2, int, S_IDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, ent, int, S_IDX2, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, ent2, int, S_MISC2, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, erow, int, S_MISC3, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dlu, int, S_NNLU, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, ulu, int, S_OUT1, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, du, int, S_OUT2, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dui, int, S_OUT3, (size_t)(nI > 0 ? nI : 1));
+  if (nI > 0) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(keys, nnIndx, sizeof(int) * nI, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dlu, nnIndxLU, sizeof(int) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemsetAsync(ulu + n, 0, sizeof(int) * n, ctx->stream));
+  if (nI > 0) {
+    entry_row_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(n, dlu, erow);
+    NNGP_LAUNCH_CHECK(ctx);
+    iota_kernel<<<blocks(nI, 256), 256, 0, ctx->stream>>>(ent, nI);
+    NNGP_LAUNCH_CHECK(ctx);
+    count_kernel<<<blocks(nI, 256), 256, 0, ctx->stream>>>(keys, nI, ulu + n);
+    NNGP_LAUNCH_CHECK(ctx);
+    size_t tmp = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys, keys2, ent, ent2, (int)nI, 0, 32, ctx->stream);
+    size_t tmp2 = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tmp2, ulu + n, ulu, n, ctx->stream);
+    void *dtmp;
+    NNGP_ALLOC(ctx, dtmp, unsigned char, S_SORT_TMP, tmp > tmp2 ? tmp : tmp2);
+    NNGP_CUDA_TRY(ctx, cub::DeviceRadixSort::SortPairs(dtmp, tmp, keys, keys2, ent, ent2, (int)nI, 0, 32, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cub::DeviceScan::ExclusiveSum(dtmp, tmp2, ulu + n, ulu, n, ctx->stream));
+    ctx->launches += 2;
+    uindx_fill_kernel<<<blocks(nI, 256), 256, 0, ctx->stream>>>(nI, ent2, erow, dlu, du, dui);
+    NNGP_LAUNCH_CHECK(ctx);
+    if (searchType == 1) {
+      reverse_segments_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(n, ulu, du, dui);
+      NNGP_LAUNCH_CHECK(ctx);
+    }
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(uIndx, du, sizeof(int) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(uiIndx, dui, sizeof(int) * nI, cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    NNGP_CUDA_TRY(ctx, cudaMemsetAsync(ulu, 0, sizeof(int) * n, ctx->stream));
+  }
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(uIndxLU, ulu, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,555 @@
+// Response-model MCMC (reference rNNGP, src/rNNGP.cpp:103-421) on the device.
+//
+// The chain stays sequential over iterations; everything inside an iteration
+// runs on the GPU, for one or many independent instances at once:
+//   mc_pre    (one thread per instance) beta | theta from the cached Gram of the
+//             current theta (p x p potrf/potri/symv/potrf, src/rNNGP.cpp:274-292),
+//             beta draw (src/util.cpp:28-41), log target at the current theta,
+//             Metropolis proposals (src/rNNGP.cpp:327-333) written as the
+//             candidate's CovParams;
+//   B/F pass  the fused likelihood pass at the candidate for all instances
+//             (log F and the Gram of [X y], no B written);
+//   mc_post   (one thread per instance) log target at the candidate, accept /
+//             reject on the next uniform (src/rNNGP.cpp:349-354), samples saved.
+// The reference recomputes updateBF at the current theta every iteration
+// (src/rNNGP.cpp:306); that recomputation is deterministic, so the current
+// theta's log-determinant and Gram are cached instead, which halves the solves
+// without changing any value.  Q(X beta - y) comes from the Gram:
+// beta'Gxx beta - 2 beta'Gxy + Gyy.  Iterations with a replicate draw
+// (fit.rep) additionally run the standalone B/F pass at the current theta and
+// the sequential recurrence of src/rNNGP.cpp:24-42.
+// Random numbers come from host-fed streams in the reference's order.  Each
+// iteration is captured once as a CUDA graph and replayed.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <vector>
+#include "nngp_internal.h"
+#include "nngp_small.cuh"
+
+namespace {
+
+constexpr int PMAX = NNGP_MAX_NV - 1;
+
+struct MCConst {
+  int n, p, model, nTheta, nSamples;
+  double sIG[2], tIG[2], pU[2], nU[2], tuning[4];
+  const double *normals;
+  long long nNormals;
+  const double *unifs;
+  long long nUnifs;
+  const int *repIndx;  // may be null
+  double *betaOut;     // p x nSamples
+  double *thetaOut;    // nTheta x nSamples
+  double *repOut;      // n x nRep
+  const double *X;     // n x p column-major
+  const double *B;     // standalone pass outputs (replicates)
+  const double *F;
+  const int *nnIndx, *nnLU;
+};
+
+struct MCState {
+  double theta[4], cand[4];
+  double beta[PMAX], mean[PMAX], L[PMAX * PMAX];
+  double G[NNGP_MAX_NV * NNGP_MAX_NV];
+  double ld, lpCur;
+  long long npos, upos, repStart;
+  int thetaUpdate, accept, s, repCnt, status, doRep;
+};
+
+__device__ inline bool next_normal(const MCConst &c, MCState &st, double &z) {
+  if (st.npos >= c.nNormals) {
+    st.status = 3;
+    z = 0.0;
+    return false;
+  }
+  z = c.normals[st.npos++];
+  return true;
+}
+// R's rnorm(mu, sd): consumes a draw only when sd > 0 and mu is finite.
+__device__ inline double r_rnorm(const MCConst &c, MCState &st, double mu, double sd) {
+  if (isnan(mu) || !isfinite(sd) || sd < 0.0) return nan("");
+  if (sd == 0.0 || !isfinite(mu)) return mu;
+  double z;
+  next_normal(c, st, z);
+  return mu + sd * z;
+}
+__device__ inline double logit(double t, double a, double b) { return log((t - a) / (b - t)); }
+__device__ inline double logit_inv(double z, double a, double b) { return b - (b - a) / (1 + exp(z)); }
+
+__device__ inline double log_post(const MCConst &c, double ld, double q, const double *th) {
+  double lp = -0.5 * ld - 0.5 * q;
+  lp += log(th[2] - c.pU[0]) + log(c.pU[1] - th[2]);
+  lp += -1.0 * (1.0 + c.sIG[0]) * log(th[0]) - c.sIG[1] / th[0] + log(th[0]);
+  lp += -1.0 * (1.0 + c.tIG[0]) * log(th[1]) - c.tIG[1] / th[1] + log(th[1]);
+  if (c.model == 2) lp += log(th[3] - c.nU[0]) + log(c.nU[1] - th[3]);
+  return lp;
+}
+
+// Q(X beta - y) from the Gram G of V = [X y] (nv = p + 1, column-major).
+__device__ inline double quad_from_gram(const double *G, int p, const double *beta) {
+  const int nv = p + 1;
+  double q = G[p * nv + p];
+  for (int a = 0; a < p; a++) {
+    q -= 2.0 * beta[a] * G[p * nv + a];
+    for (int b = 0; b < p; b++) q += beta[a] * G[b * nv + a] * beta[b];
+  }
+  return q;
+}
+
+__device__ inline void set_params(CovParams &cp, int model, const double *th) {
+  cp.model = model;
+  cp.sigmaSq = th[0];
+  cp.tauSq = th[1];
+  cp.phi = th[2];
+  cp.nu = model == 2 ? th[3] : 0.0;
+  cov_prepare(cp);
+}
+
+// Unpacks nngp_bf_run's (log F, upper-triangle Gram) sums.
+__device__ inline void unpack(const double *o, int nv, double &ld, double *G) {
+  ld = o[0];
+  int k = 1;
+  for (int a = 0; a < nv; a++)
+    for (int b = a; b < nv; b++) {
+      G[b * nv + a] = o[k];
+      G[a * nv + b] = o[k];
+      k++;
+    }
+}
+
+__global__ void mc_init_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts,
+                               const double *__restrict__ out, int ng, int ninst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ninst) return;
+  MCState &st = sts[k];
+  unpack(out + (size_t)k * ng, cs[k].p + 1, st.ld, st.G);
+  st.thetaUpdate = 1;
+}
+
+__global__ void mc_pre_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts,
+                              CovParams *__restrict__ thetas, int ninst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ninst) return;
+  const MCConst &c = cs[k];
+  MCState &st = sts[k];
+  if (st.status || st.s >= c.nSamples) return;
+  const int p = c.p, nv = p + 1;
+  if (st.thetaUpdate) {
+    st.thetaUpdate = 0;
+    double V[PMAX * PMAX], g[PMAX];
+    for (int i = 0; i < p; i++) {
+      g[i] = st.G[p * nv + i];
+      for (int j = 0; j < p; j++) V[j * p + i] = (j <= i) ? st.G[j * nv + i] : 0.0;
+    }
+    if (!small_potrf(V, p)) {
+      st.status = 2;
+      return;
+    }
+    small_potri(V, p);
+    small_symv(V, p, g, st.mean);
+    if (!small_potrf(V, p)) {
+      st.status = 2;
+      return;
+    }
+    for (int i = 0; i < p * p; i++) st.L[i] = V[i];
+  }
+  // beta ~ N(mean, L L'): z then L z + mean
+  double z[PMAX];
+  for (int i = 0; i < p; i++) z[i] = r_rnorm(c, st, 0.0, 1.0);
+  for (int i = 0; i < p; i++) {
+    double s = st.mean[i];
+    for (int j = 0; j <= i; j++) s += st.L[j * p + i] * z[j];
+    st.beta[i] = s;
+  }
+  // replicate draw at the current theta consumes n normals here
+  st.doRep = (c.repIndx && c.repIndx[st.s]) ? 1 : 0;
+  if (st.doRep) {
+    st.repStart = st.npos;
+    if (st.npos + c.n > c.nNormals) st.status = 3;
+    st.npos += c.n;
+  }
+  const double q = quad_from_gram(st.G, p, st.beta);
+  st.lpCur = log_post(c, st.ld, q, st.theta);
+  // proposals in the reference's order: phi, sigma^2, tau^2, nu
+  st.cand[2] = logit_inv(r_rnorm(c, st, logit(st.theta[2], c.pU[0], c.pU[1]), c.tuning[2]), c.pU[0], c.pU[1]);
+  st.cand[0] = exp(r_rnorm(c, st, log(st.theta[0]), c.tuning[0]));
+  st.cand[1] = exp(r_rnorm(c, st, log(st.theta[1]), c.tuning[1]));
+  if (c.model == 2)
+    st.cand[3] = logit_inv(r_rnorm(c, st, logit(st.theta[3], c.nU[0], c.nU[1]), c.tuning[3]), c.nU[0], c.nU[1]);
+  set_params(thetas[2 * k + 1], c.model, st.cand);
+}
+
+__global__ void mc_post_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts,
+                               CovParams *__restrict__ thetas, const double *__restrict__ out, int ng,
+                               int ninst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ninst) return;
+  const MCConst &c = cs[k];
+  MCState &st = sts[k];
+  if (st.status || st.s >= c.nSamples) return;
+  const int p = c.p, nv = p + 1;
+  double ld, G[NNGP_MAX_NV * NNGP_MAX_NV];
+  unpack(out + (size_t)k * ng, nv, ld, G);
+  const double q = quad_from_gram(G, p, st.beta);
+  const double lpCand = log_post(c, ld, q, st.cand);
+  double u = 0.5;
+  if (st.upos >= c.nUnifs) st.status = 3;
+  else u = c.unifs[st.upos++];
+  if (u <= exp(lpCand - st.lpCur)) {
+    st.thetaUpdate = 1;
+    for (int t = 0; t < 4; t++) st.theta[t] = st.cand[t];
+    st.ld = ld;
+    for (int t = 0; t < nv * nv; t++) st.G[t] = G[t];
+    thetas[2 * k] = thetas[2 * k + 1];
+    st.accept++;
+  }
+  for (int i = 0; i < p; i++) c.betaOut[(size_t)st.s * p + i] = st.beta[i];
+  for (int t = 0; t < c.nTheta; t++) c.thetaOut[(size_t)st.s * c.nTheta + t] = st.theta[t];
+  st.s++;
+}
+
+// Replicate: v_i = B_i v_N(i) + sqrt(F_i) z_i sequentially, y_rep = X beta + v.
+__global__ void mc_rep_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts, int ninst) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ninst) return;
+  const MCConst &c = cs[k];
+  MCState &st = sts[k];
+  if (st.status || !st.doRep) return;
+  double *out = c.repOut + (size_t)st.repCnt * c.n;
+  const double *z = c.normals + st.repStart;
+  const int n = c.n;
+  for (int i = 0; i < n; i++) {
+    double v = sqrt(c.F[i]) * z[i];
+    const int off = c.nnLU[i], cnt = c.nnLU[n + i];
+    double s = 0.0;
+    for (int j = 0; j < cnt; j++) s += c.B[off + j] * out[c.nnIndx[off + j]];
+    out[i] = (i == 0) ? v : s + v;
+  }
+  // the recurrence read out[] as v; now add X beta
+  for (int i = 0; i < n; i++) {
+    double xb = 0.0;
+    for (int j = 0; j < c.p; j++) xb += c.X[(size_t)j * n + i] * st.beta[j];
+    out[i] += xb;
+  }
+  st.repCnt++;
+}
+
+// Every block of the standalone pass checks whether this iteration draws a replicate.
+__global__ void noop_kernel() {}
+
+__global__ void interleave_kernel2(const double *__restrict__ cm, int n, double *__restrict__ xy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    xy[2 * i] = cm[i];
+    xy[2 * i + 1] = cm[n + i];
+  }
+}
+
+__global__ void build_v_kernel(const double *__restrict__ X, const double *__restrict__ y, int n, int p,
+                               double *__restrict__ V) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nv = p + 1;
+  if (t < (long)n * nv) {
+    const int i = (int)(t / nv), v = (int)(t % nv);
+    V[t] = (v < p) ? X[(size_t)v * n + i] : y[i];
+  }
+}
+
+inline unsigned nblk(long cnt, int tpb) { return (unsigned)((cnt + tpb - 1) / tpb); }
+
+}  // namespace
+
+// One instance of the response model as the batched driver takes it (device pointers).
+struct MCInstance {
+  int n, m, p, model;
+  const double *coords_cm;  // n x 2 column-major
+  const int *nnIndx, *nnLU;
+  const double *X, *y;      // X n x p column-major
+  double sIG[2], tIG[2], pU[2], nU[2];
+  double betaStart[PMAX], thetaStart[4], tuning[4];
+  int nSamples;
+  const double *normals;
+  long long nNormals;
+  const double *unifs;
+  long long nUnifs;
+  const int *repIndx;       // device, nSamples entries, or null
+  double *betaOut, *thetaOut, *repOut;
+};
+
+// Runs nSamples iterations for every instance (all instances share p).
+int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int precision,
+                  const std::vector<int> *host_rep, int *accept_out) {
+  const int ninst = (int)insts.size();
+  if (ninst == 0) return NNGP_OK;
+  const int p = insts[0].p, nv = p + 1, ng = 1 + nv * (nv + 1) / 2;
+  int nS = 0;
+  for (const auto &I : insts) nS = I.nSamples > nS ? I.nSamples : nS;
+  std::vector<void *> owned;
+  auto own = [&](size_t bytes) {
+    void *q = nngp_malloc_async(ctx, bytes);
+    owned.push_back(q);
+    return q;
+  };
+  auto release = [&]() {
+    for (void *q : owned) nngp_free_async(ctx, q);
+  };
+  std::vector<BFData> datas(ninst);
+  std::vector<MCConst> consts(ninst);
+  std::vector<MCState> states(ninst);
+  std::vector<CovParams> th(2 * ninst);
+  const bool anyRep = host_rep != nullptr;
+  for (int k = 0; k < ninst; k++) {
+    const MCInstance &I = insts[k];
+    if (I.p != p) return nngp_fail(ctx, NNGP_ERR_ARG, "instances of one batch must share p");
+    double *xy = (double *)own(sizeof(double) * 2 * I.n);
+    double *V = (double *)own(sizeof(double) * (size_t)I.n * nv);
+    if (!xy || !V) {
+      release();
+      return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+    }
+    interleave_kernel2<<<nblk(I.n, 256), 256, 0, ctx->stream>>>(I.coords_cm, I.n, xy);
+    build_v_kernel<<<nblk((long)I.n * nv, 256), 256, 0, ctx->stream>>>(I.X, I.y, I.n, p, V);
+    ctx->launches += 2;
+    BFData d{};
+    d.n = I.n;
+    d.m = I.m;
+    d.nv = nv;
+    d.xy = xy;
+    d.nnIndx = I.nnIndx;
+    d.nnLU = I.nnLU;
+    d.V = V;
+    if (anyRep) {
+      const int64_t nI = nngp_nindx(I.n, I.m);
+      d.B = (double *)own(sizeof(double) * (nI > 0 ? nI : 1));
+      d.F = (double *)own(sizeof(double) * I.n);
+    }
+    datas[k] = d;
+    MCConst &c = consts[k];
+    c = MCConst{};
+    c.n = I.n;
+    c.p = p;
+    c.model = I.model;
+    c.nTheta = I.model == 2 ? 4 : 3;
+    c.nSamples = I.nSamples;
+    for (int t = 0; t < 2; t++) {
+      c.sIG[t] = I.sIG[t];
+      c.tIG[t] = I.tIG[t];
+      c.pU[t] = I.pU[t];
+      c.nU[t] = I.nU[t];
+    }
+    for (int t = 0; t < 4; t++) c.tuning[t] = I.tuning[t];
+    c.normals = I.normals;
+    c.nNormals = I.nNormals;
+    c.unifs = I.unifs;
+    c.nUnifs = I.nUnifs;
+    c.repIndx = I.repIndx;
+    c.betaOut = I.betaOut;
+    c.thetaOut = I.thetaOut;
+    c.repOut = I.repOut;
+    c.X = I.X;
+    c.B = d.B;
+    c.F = d.F;
+    c.nnIndx = I.nnIndx;
+    c.nnLU = I.nnLU;
+    MCState &s = states[k];
+    s = MCState{};
+    for (int t = 0; t < 4; t++) s.theta[t] = s.cand[t] = I.thetaStart[t];
+    for (int t = 0; t < p; t++) s.beta[t] = I.betaStart[t];
+    CovParams cp{};
+    cp.model = I.model;
+    cp.sigmaSq = I.thetaStart[0];
+    cp.tauSq = I.thetaStart[1];
+    cp.phi = I.thetaStart[2];
+    cp.nu = I.model == 2 ? I.thetaStart[3] : 0.0;
+    cov_prepare(cp);
+    th[2 * k] = th[2 * k + 1] = cp;
+  }
+  MCConst *d_c = (MCConst *)own(sizeof(MCConst) * ninst);
+  MCState *d_s = (MCState *)own(sizeof(MCState) * ninst);
+  CovParams *d_th = (CovParams *)own(sizeof(CovParams) * 2 * ninst);
+  double *d_out = (double *)own(sizeof(double) * 2 * (size_t)ninst * ng);
+  double *d_out0 = (double *)own(sizeof(double) * 2 * (size_t)ninst);
+  unsigned long long *d_status = (unsigned long long *)own(sizeof(unsigned long long));
+  if (!d_c || !d_s || !d_th || !d_out || !d_out0 || !d_status) {
+    release();
+    return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  }
+  int st = NNGP_OK;
+#define MC_TRY(expr)                                                  \
+  do {                                                                \
+    cudaError_t e_ = (expr);                                          \
+    if (e_ != cudaSuccess) {                                          \
+      release();                                                      \
+      return nngp_fail(ctx, NNGP_ERR_CUDA, std::string(#expr ": ") + cudaGetErrorString(e_)); \
+    }                                                                 \
+  } while (0)
+  MC_TRY(cudaMemcpyAsync(d_c, consts.data(), sizeof(MCConst) * ninst, cudaMemcpyHostToDevice, ctx->stream));
+  MC_TRY(cudaMemcpyAsync(d_s, states.data(), sizeof(MCState) * ninst, cudaMemcpyHostToDevice, ctx->stream));
+  MC_TRY(cudaMemcpyAsync(d_th, th.data(), sizeof(CovParams) * 2 * ninst, cudaMemcpyHostToDevice, ctx->stream));
+  if ((st = nngp_reset_status(ctx, d_status))) {
+    release();
+    return st;
+  }
+  // plans: fused pass at each instance's candidate slot; standalone pass at the current slot
+  std::vector<PassEval> evCand(ninst), evCur(ninst);
+  for (int k = 0; k < ninst; k++) {
+    evCand[k] = PassEval{k, 2 * k + 1};
+    evCur[k] = PassEval{k, 2 * k};
+  }
+  BFPlan planCand, planCur;
+  if ((st = nngp_bf_plan(ctx, &planCand, precision, 1, nv, datas, d_th, evCand, d_status))) {
+    release();
+    return st;
+  }
+  if (anyRep && (st = nngp_bf_plan(ctx, &planCur, precision, 0, 0, datas, d_th, evCur, d_status))) {
+    nngp_bf_plan_free(ctx, &planCand);
+    release();
+    return st;
+  }
+  // initial state: likelihood pass at the starting theta (candidate slot = start)
+  st = nngp_bf_run(ctx, &planCand, d_out);
+  if (!st) {
+    mc_init_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_out, ng, ninst);
+    ctx->launches++;
+  }
+  // one iteration as a graph (with and without the replicate draw)
+  auto capture = [&](bool rep, cudaGraphExec_t *exec) -> int {
+    cudaGraph_t g;
+    MC_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int s2 = NNGP_OK;
+    mc_pre_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
+    if (rep) {
+      s2 = nngp_bf_run(ctx, &planCur, d_out0);
+      mc_rep_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
+    }
+    if (!s2) s2 = nngp_bf_run(ctx, &planCand, d_out);
+    mc_post_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, d_out, ng, ninst);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (s2) return s2;
+    if (e != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    return NNGP_OK;
+  };
+  cudaGraphExec_t gPlain = nullptr, gRep = nullptr;
+  const int64_t launches_before = ctx->launches;
+  if (!st) st = capture(false, &gPlain);
+  const int64_t per_plain = ctx->launches - launches_before;
+  int64_t per_rep = 0;
+  if (!st && anyRep) {
+    const int64_t b = ctx->launches;
+    st = capture(true, &gRep);
+    per_rep = ctx->launches - b;
+  }
+  ctx->launches = launches_before;  // captured launches are counted when replayed below
+  for (int s = 0; !st && s < nS; s++) {
+    const bool rep = anyRep && (*host_rep)[s] != 0;
+    cudaError_t e = cudaGraphLaunch(rep ? gRep : gPlain, ctx->stream);
+    if (e != cudaSuccess) st = nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+    ctx->launches += rep ? per_rep : per_plain;
+  }
+  if (!st) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) st = nngp_fail(ctx, NNGP_ERR_CUDA, std::string("mcmc: ") + cudaGetErrorString(e));
+  }
+  if (gPlain) cudaGraphExecDestroy(gPlain);
+  if (gRep) cudaGraphExecDestroy(gRep);
+  if (!st) st = nngp_check_status(ctx, d_status, "rNNGP");
+  if (!st) {
+    MC_TRY(cudaMemcpy(states.data(), d_s, sizeof(MCState) * ninst, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < ninst && !st; k++) {
+      if (accept_out) accept_out[k] = states[k].accept;
+      if (states[k].status == 2) st = nngp_fail(ctx, NNGP_ERR_NOT_SPD, "rNNGP: beta Gram matrix not positive definite (dpotrf failed)");
+      if (states[k].status == 3) st = nngp_fail(ctx, NNGP_ERR_STREAM, "rNNGP: a host-fed random stream ran out");
+    }
+  }
+  nngp_bf_plan_free(ctx, &planCand);
+  if (anyRep) nngp_bf_plan_free(ctx, &planCur);
+  release();
+  cudaStreamSynchronize(ctx->stream);
+#undef MC_TRY
+  return st;
+}
+
+extern "C" int nngp_rNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, int m,
+                          const double *coords, int covModel, const int *nnIndx, const int *nnIndxLU,
+                          const double *sigmaSqIG, const double *tauSqIG, const double *phiUnif,
+                          const double *nuUnif, const double *betaStarting, const double *thetaStarting,
+                          const double *tuning, int nSamples, int nRep, const int *repIndx,
+                          const double *normals, int64_t nNormals, const double *unifs, int64_t nUnifs,
+                          int precision, double *betaSamples, double *thetaSamples, double *repSamples,
+                          int *nAccept) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (p < 1 || p > PMAX) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= p <= 7 required");
+  if (n < 1 || m < 1 || m > NNGP_MAX_M || n < m) return nngp_fail(ctx, NNGP_ERR_ARG, "n >= m and 1 <= m <= 32 required");
+  if (covModel < 0 || covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+  if (nSamples < 0) return nngp_fail(ctx, NNGP_ERR_ARG, "n.samples must be >= 0");
+  cudaSetDevice(ctx->device);
+  const int nTheta = covModel == 2 ? 4 : 3;
+  const int64_t nI = nngp_nindx(n, m);
+  std::vector<void *> tmp;
+  auto up = [&](const void *h, size_t bytes) -> void * {
+    void *d = nngp_malloc_async(ctx, bytes ? bytes : 16);
+    if (d && bytes && h) cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    tmp.push_back(d);
+    return d;
+  };
+  auto fin = [&](int status) {
+    for (void *q : tmp) nngp_free_async(ctx, q);
+    cudaStreamSynchronize(ctx->stream);
+    return status;
+  };
+  MCInstance I{};
+  I.n = n;
+  I.m = m;
+  I.p = p;
+  I.model = covModel;
+  I.coords_cm = (const double *)up(coords, sizeof(double) * 2 * n);
+  I.nnIndx = (const int *)up(nnIndx, sizeof(int) * (nI > 0 ? nI : 0));
+  I.nnLU = (const int *)up(nnIndxLU, sizeof(int) * 2 * n);
+  I.X = (const double *)up(X, sizeof(double) * (size_t)n * p);
+  I.y = (const double *)up(y, sizeof(double) * n);
+  for (int t = 0; t < 2; t++) {
+    I.sIG[t] = sigmaSqIG[t];
+    I.tIG[t] = tauSqIG[t];
+    I.pU[t] = phiUnif[t];
+    I.nU[t] = covModel == 2 ? nuUnif[t] : 0.0;
+  }
+  for (int t = 0; t < p; t++) I.betaStart[t] = betaStarting[t];
+  for (int t = 0; t < 4; t++) {
+    I.thetaStart[t] = t < nTheta ? thetaStarting[t] : 0.0;
+    I.tuning[t] = t < nTheta ? tuning[t] : 0.0;
+  }
+  I.nSamples = nSamples;
+  I.normals = (const double *)up(normals, sizeof(double) * (size_t)nNormals);
+  I.nNormals = nNormals;
+  I.unifs = (const double *)up(unifs, sizeof(double) * (size_t)nUnifs);
+  I.nUnifs = nUnifs;
+  std::vector<int> hrep;
+  if (nRep > 0) {
+    I.repIndx = (const int *)up(repIndx, sizeof(int) * nSamples);
+    hrep.assign(repIndx, repIndx + nSamples);
+  }
+  I.betaOut = (double *)up(nullptr, sizeof(double) * (size_t)p * (nSamples ? nSamples : 1));
+  I.thetaOut = (double *)up(nullptr, sizeof(double) * (size_t)nTheta * (nSamples ? nSamples : 1));
+  I.repOut = nRep > 0 ? (double *)up(nullptr, sizeof(double) * (size_t)n * nRep) : nullptr;
+  for (void *q : tmp)
+    if (!q) return fin(nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed"));
+  if (nSamples == 0) {
+    if (nAccept) *nAccept = 0;
+    return fin(NNGP_OK);
+  }
+  int acc = 0;
+  int st = nngp_run_mcmc(ctx, {I}, precision, nRep > 0 ? &hrep : nullptr, &acc);
+  if (st) return fin(st);
+  if (nAccept) *nAccept = acc;
+  cudaMemcpyAsync(betaSamples, I.betaOut, sizeof(double) * (size_t)p * nSamples, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaMemcpyAsync(thetaSamples, I.thetaOut, sizeof(double) * (size_t)nTheta * nSamples, cudaMemcpyDeviceToHost,
+                  ctx->stream);
+  if (nRep > 0 && repSamples)
+    cudaMemcpyAsync(repSamples, I.repOut, sizeof(double) * (size_t)n * nRep, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fin(nngp_fail(ctx, NNGP_ERR_CUDA, cudaGetErrorString(e)));
+  return fin(NNGP_OK);
+}

@@ -1,0 +1,45 @@
+"""The C ABI: the library builds, loads without a GPU, and exports every symbol
+the public header declares.  CPU only (no compute calls)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "spnngp_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(nngp_[A-Za-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for must in ("nngp_mkNNIndxCB", "nngp_mkNNIndx", "nngp_mkUIndx", "nngp_updateBF", "nngp_updateConjBF",
+                 "nngp_Q", "nngp_rNNGP", "nngp_cNNGP", "nngp_rNNGPPredict", "nngp_rNNGPReplicated"):
+        assert must in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from spnngp_gb300.build import build
+
+    path = build()
+    lib = ctypes.CDLL(path)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_package_import_does_not_touch_gpu():
+    import spnngp_gb300
+
+    assert spnngp_gb300.COV_MODELS == ("exponential", "spherical", "matern", "gaussian")
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    from spnngp_gb300 import _lib
+
+    with pytest.raises(ImportError):
+        _lib._Lib(str(tmp_path / "nope.so"))
