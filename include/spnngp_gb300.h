@@ -190,6 +190,18 @@ int nngp_loglik_gram_dev(nngp_ctx *ctx, int n, int m, int nv, const double *coor
 int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
                         double *nnDist, int *nnIndxLU);
 
+/* Measurement utility, no counterpart in the reference: sustained FMA
+ * throughput (FLOP/s) of the FP64 (fp64 != 0) or FP32 CUDA-core pipe, the
+ * denominator of the B/F pass's roofline fraction. */
+int nngp_measure_peak(nngp_ctx *ctx, int fp64, double *flops_per_s);
+
+/* Measurement utility, no counterpart in the reference: when on, CUDA events
+ * are recorded on the launching stream around every primary launch of the B/F
+ * pass kernel; nngp_kernel_time returns (and clears) their summed duration in
+ * milliseconds and the number of launches timed. */
+int nngp_set_kernel_timing(nngp_ctx *ctx, int on);
+int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,6 +56,9 @@ _SIGNATURES = {
     "nngp_updateBF_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp, _vp]),
     "nngp_loglik_gram_dev": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp]),
     "nngp_mkNNIndxCB_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
+    "nngp_measure_peak": (_i, [_vp, _i, _dp]),
+    "nngp_set_kernel_timing": (_i, [_vp, _i]),
+    "nngp_kernel_time": (_i, [_vp, _dp, C.POINTER(_i64)]),
 }
 
 

@@ -171,5 +171,135 @@ def loglik_gram(coords, nn_indx, nn_indx_lu, m: int, V, cov_model, theta, precis
     return float(ld[0]), G.reshape(nv, nv)
 
 
+# ------------------------------------------------------------------ drivers
+
+def rNNGP(y, X, m: int, coords, cov_model, nn_indx, nn_indx_lu, sigma_sq_IG, tau_sq_IG, phi_unif, nu_unif,
+          beta_starting, theta_starting, tuning, n_samples: int, normals, unifs, n_rep: int = 0, rep_indx=None,
+          precision="fp64", ctx: Context | None = None) -> dict:
+    """Response-model MCMC, the .Call("rNNGP", ...) routine (src/rNNGP.cpp:103-421).
+
+    theta_starting / tuning are (sigma.sq, tau.sq, phi[, nu]).  normals / unifs are the host-fed
+    streams consumed in the reference's order (p normals for beta, n for a replicate draw, one per
+    proposal with non-zero tuning, one uniform per iteration).  Returns p.beta.samples (p x n),
+    p.theta.samples (nTheta x n), y.rep.samples (n x n.rep) and the acceptance count."""
+    y = f64(y)
+    n = len(y)
+    Xa = np.asarray(X, np.float64)
+    Xc = f64(Xa.T.reshape(-1)) if Xa.ndim == 2 else f64(Xa)
+    p = len(Xc) // n
+    c = coords_cm(coords)
+    model = cov_model_index(cov_model)
+    nTheta = 4 if model == 2 else 3
+    ts = f64(list(np.asarray(theta_starting, np.float64).reshape(-1)[:nTheta]) + [0.0] * (4 - nTheta))
+    tu = f64(list(np.asarray(tuning, np.float64).reshape(-1)[:nTheta]) + [0.0] * (4 - nTheta))
+    nu_u = f64(nu_unif if nu_unif is not None else [0.0, 0.0])
+    normals, unifs = f64(normals), f64(unifs)
+    ri = i32(rep_indx if rep_indx is not None else np.zeros(max(1, n_samples), np.int32))
+    beta_s = np.zeros(max(1, p * n_samples))
+    theta_s = np.zeros(max(1, nTheta * n_samples))
+    rep = np.zeros(max(1, n * n_rep))
+    acc = np.zeros(1, np.int32)
+    _ctx(ctx).call("nngp_rNNGP", dptr(y), dptr(Xc), p, n, m, dptr(c), model, iptr(i32(nn_indx)),
+                   iptr(i32(nn_indx_lu)), dptr(f64(sigma_sq_IG)), dptr(f64(tau_sq_IG)), dptr(f64(phi_unif)),
+                   dptr(nu_u), dptr(f64(beta_starting)), dptr(ts), dptr(tu), int(n_samples), int(n_rep), iptr(ri),
+                   dptr(normals), len(normals), dptr(unifs), len(unifs), precision_code(precision), dptr(beta_s),
+                   dptr(theta_s), dptr(rep), iptr(acc))
+    out = {"p.beta.samples": beta_s[: p * n_samples].reshape(n_samples, p).T,
+           "p.theta.samples": theta_s[: nTheta * n_samples].reshape(n_samples, nTheta).T,
+           "accept": int(acc[0])}
+    if n_rep:
+        out["y.rep.samples"] = rep[: n * n_rep].reshape(n_rep, n).T
+    return out
+
+
+def cNNGP(y, X, coords, theta_alpha, nn_indx, nn_indx_lu, X0, coords0, nn_indx0, m: int, sigma_sq_IG, cov_model,
+          precision="fp64", ctx: Context | None = None) -> dict:
+    """Conjugate NNGP over the columns of theta_alpha (nTheta x g, rows phi, alpha[, nu]) with prediction at
+    coords0 -- the .Call("cNNGP", ...) routine (src/cNNGP.cpp:73-358).  nn_indx0 is n0 x m, 0-based."""
+    y = f64(y)
+    n = len(y)
+    Xa = np.asarray(X, np.float64)
+    Xc = f64(Xa.T.reshape(-1)) if Xa.ndim == 2 else f64(Xa)
+    p = len(Xc) // n
+    c = coords_cm(coords)
+    model = cov_model_index(cov_model)
+    nTheta = 3 if model == 2 else 2
+    ta = np.asarray(theta_alpha, np.float64)
+    ta = f64(ta.T.reshape(-1)) if ta.ndim == 2 else f64(ta)
+    g = len(ta) // nTheta
+    if coords0 is not None and len(np.asarray(coords0)):
+        c0 = coords_cm(coords0)
+        n0 = len(c0) // 2
+        X0a = np.asarray(X0, np.float64)
+        X0c = f64(X0a.T.reshape(-1)) if X0a.ndim == 2 else f64(X0a)
+        nn0 = np.asarray(nn_indx0)
+        nn0 = i32(nn0.T.reshape(-1)) if nn0.ndim == 2 else i32(nn0)
+    else:
+        n0, c0, X0c, nn0 = 0, np.zeros(2), np.zeros(1), np.zeros(1, np.int32)
+    beta = np.zeros(p * g)
+    ab = np.zeros(2 * g)
+    bBInv = np.zeros(p * p * g)
+    bb = np.zeros(p * g)
+    y0 = np.zeros(max(1, n0 * g))
+    y0v = np.zeros(max(1, n0 * g))
+    _ctx(ctx).call("nngp_cNNGP", dptr(y), dptr(Xc), p, n, dptr(c), dptr(ta), iptr(i32(nn_indx)), iptr(i32(nn_indx_lu)),
+                   dptr(X0c), dptr(c0), n0, iptr(nn0), g, m, dptr(f64(sigma_sq_IG)), model, precision_code(precision),
+                   dptr(beta), dptr(ab), dptr(bBInv), dptr(bb), dptr(y0), dptr(y0v))
+    out = {"beta.hat": beta.reshape(g, p).T, "ab": ab.reshape(g, 2).T, "bB.inv": bBInv.reshape(g, p * p).T,
+           "bb": bb.reshape(g, p).T}
+    if n0:
+        out["y.0.hat"] = y0[: n0 * g].reshape(g, n0).T
+        out["y.0.hat.var"] = y0v[: n0 * g].reshape(g, n0).T
+    return out
+
+
+def rNNGPPredict(X, y, coords, m: int, X0, coords0, nn_indx0, beta_samples, theta_samples, cov_model, z,
+                 precision="fp64", ctx: Context | None = None) -> dict:
+    """Posterior predictive draws (src/rNNGPPredict.cpp:25-223).  beta_samples p x nS, theta_samples
+    nTheta x nS, z q*nS normals with z[i*nS + s] for (point i, sample s).  Returns p.y.0 (q x nS)."""
+    y = f64(y)
+    n = len(y)
+    Xa = np.asarray(X, np.float64)
+    Xc = f64(Xa.T.reshape(-1)) if Xa.ndim == 2 else f64(Xa)
+    p = len(Xc) // n
+    c = coords_cm(coords)
+    c0 = coords_cm(coords0)
+    q = len(c0) // 2
+    X0a = np.asarray(X0, np.float64)
+    X0c = f64(X0a.T.reshape(-1)) if X0a.ndim == 2 else f64(X0a)
+    nn0 = np.asarray(nn_indx0)
+    nn0 = i32(nn0.T.reshape(-1)) if nn0.ndim == 2 else i32(nn0)
+    bs = np.asarray(beta_samples, np.float64)
+    nS = bs.size // p
+    bsc = f64(bs.T.reshape(-1)) if bs.ndim == 2 else f64(bs)
+    ts = np.asarray(theta_samples, np.float64)
+    tsc = f64(ts.T.reshape(-1)) if ts.ndim == 2 else f64(ts)
+    y0 = np.zeros(max(1, q * nS))
+    _ctx(ctx).call("nngp_rNNGPPredict", dptr(Xc), dptr(y), dptr(c), n, p, m, dptr(X0c), dptr(c0), q, iptr(nn0),
+                   dptr(bsc), dptr(tsc), nS, cov_model_index(cov_model), dptr(f64(z)), precision_code(precision),
+                   dptr(y0))
+    return {"p.y.0": y0[: q * nS].reshape(nS, q).T}
+
+
+def rNNGPReplicated(X, m: int, coords, cov_model, nn_indx, nn_indx_lu, beta, theta, normals, precision="fp64",
+                    ctx: Context | None = None) -> dict:
+    """Replicated data at every sample (src/rNNGPReplicated.cpp:74-244).  beta nS x p, theta nTheta x nS,
+    normals n*nS consumed sample by sample.  Returns y.rep.samples (n x nS)."""
+    c = coords_cm(coords)
+    n = len(c) // 2
+    Xa = np.asarray(X, np.float64)
+    Xc = f64(Xa.T.reshape(-1)) if Xa.ndim == 2 else f64(Xa)
+    p = len(Xc) // n
+    b = np.asarray(beta, np.float64)
+    nS = b.shape[0]
+    ts = np.asarray(theta, np.float64)
+    tsc = f64(ts.T.reshape(-1)) if ts.ndim == 2 else f64(ts)
+    yr = np.zeros(n * nS)
+    _ctx(ctx).call("nngp_rNNGPReplicated", dptr(Xc), p, n, m, dptr(c), cov_model_index(cov_model),
+                   iptr(i32(nn_indx)), iptr(i32(nn_indx_lu)), dptr(f64(b.T.reshape(-1))), dptr(tsc), nS,
+                   dptr(f64(normals)), precision_code(precision), dptr(yr))
+    return {"y.rep.samples": yr.reshape(nS, n).T}
+
+
 __all__ = ["mkNNIndxCB", "mkNNIndx", "mkUIndx", "nn2", "updateBF", "updateConjBF", "Q", "loglik_gram",
-           "cov_model_index", "precision_code", "coords_cm", "NNGPError", "Context", "COV_MODELS"]
+           "rNNGP", "cNNGP", "rNNGPPredict", "rNNGPReplicated", "cov_model_index", "precision_code", "coords_cm", "NNGPError", "Context", "COV_MODELS"]

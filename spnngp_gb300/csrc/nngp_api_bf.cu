@@ -122,11 +122,24 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   d.V = Vrm;
   d.B = d_B;
   d.F = d_F;
-  BFPlan plan;
-  st = nngp_bf_plan(ctx, &plan, precision, mode, nv, {d}, d_theta, {PassEval{0, 0}}, d_status);
-  if (!st) st = nngp_bf_run(ctx, &plan, d_out);
+  char key[256];
+  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p", mode, precision, n, m, nv, (const void *)xy,
+           (const void *)d_nnIndx, (const void *)d_nnLU, (const void *)Vrm, (void *)d_B, (void *)d_F,
+           (void *)d_theta, (void *)d_status);
+  if (!ctx->cache_plan || ctx->cache_key != key) {
+    nngp_bf_cache_release(ctx);
+    BFPlan *plan = new BFPlan();
+    st = nngp_bf_plan(ctx, plan, precision, mode, nv, {d}, d_theta, {PassEval{0, 0}}, d_status);
+    if (st) {
+      nngp_bf_plan_free(ctx, plan);
+      delete plan;
+      return st;
+    }
+    ctx->cache_plan = plan;
+    ctx->cache_key = key;
+  }
+  st = nngp_bf_run(ctx, ctx->cache_plan, d_out);
   if (!st) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, d_out, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx->stream));
-  nngp_bf_plan_free(ctx, &plan);
   if (st) return st;
   return nngp_check_status(ctx, d_status, mode == 0 ? "updateBF" : "loglik_gram");
 }

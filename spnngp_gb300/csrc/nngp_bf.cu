@@ -159,7 +159,23 @@ int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   int st;
   const bool fp32r = pl->precision == NNGP_FP32R;
   if (fp32r) NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_flags, 0, pl->flags_bytes, ctx->stream));
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (ctx->timing) {
+    for (cudaEvent_t *e : {&t0, &t1}) {
+      if (!ctx->event_pool.empty()) {
+        *e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+      } else {
+        cudaEventCreate(e);
+      }
+    }
+    cudaEventRecord(t0, ctx->stream);
+  }
   if ((st = launch_pass(ctx, pl, fp32r, false))) return st;
+  if (ctx->timing) {
+    cudaEventRecord(t1, ctx->stream);
+    ctx->timed.emplace_back(t0, t1);
+  }
   reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(pl->d_jobs, pl->ng, d_out);
   NNGP_LAUNCH_CHECK(ctx);
   if (fp32r) {
@@ -178,4 +194,35 @@ int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
 void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *pl) {
   for (void *p : pl->owned) nngp_free_async(ctx, p);
   pl->owned.clear();
+}
+
+void nngp_bf_cache_release(nngp_ctx *ctx) {
+  if (ctx->cache_plan) {
+    nngp_bf_plan_free(ctx, ctx->cache_plan);
+    delete ctx->cache_plan;
+    ctx->cache_plan = nullptr;
+    ctx->cache_key.clear();
+  }
+}
+
+extern "C" {
+int nngp_set_kernel_timing(nngp_ctx *ctx, int on) {
+  ctx->timing = on != 0;
+  return NNGP_OK;
+}
+int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches) {
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  double total = 0.0;
+  for (auto &pr : ctx->timed) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, pr.first, pr.second);
+    total += t;
+    ctx->event_pool.push_back(pr.first);
+    ctx->event_pool.push_back(pr.second);
+  }
+  if (launches) *launches = (int64_t)ctx->timed.size();
+  ctx->timed.clear();
+  if (ms) *ms = total;
+  return NNGP_OK;
+}
 }

@@ -110,9 +110,16 @@ void nngp_destroy(nngp_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  nngp_bf_cache_release(ctx);
+  cudaStreamSynchronize(ctx->stream);
   for (int s = 0; s < S_NUM_SLOTS; s++)
     if (ctx->scratch[s]) cudaFree(ctx->scratch[s]);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  for (auto &pr : ctx->timed) {
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }

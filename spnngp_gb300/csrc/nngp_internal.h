@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/spnngp_gb300.h"
@@ -27,6 +28,8 @@ enum ScratchSlot {
   S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_NUM_SLOTS
 };
 
+struct BFPlan;
+
 struct nngp_ctx {
   int device = 0;
   int sm_count = 0;
@@ -40,7 +43,15 @@ struct nngp_ctx {
   // pinned host staging for small results
   void *pinned = nullptr;
   size_t pinned_cap = 0;
+  // optional timing of the B/F kernels: events recorded around each primary launch
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed;
+  std::vector<cudaEvent_t> event_pool;
+  // last single-evaluation plan, reused while its key (pointers, sizes, mode) is unchanged
+  BFPlan *cache_plan = nullptr;
+  std::string cache_key;
 };
+void nngp_bf_cache_release(nngp_ctx *ctx);
 
 // Records an error on the context and returns the status.
 int nngp_fail(nngp_ctx *ctx, int status, const std::string &msg, int64_t loc = -1);

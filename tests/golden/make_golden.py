@@ -126,12 +126,12 @@ def main(ref_root):
     beta = rng.normal(size=(p, nS))
     theta = np.vstack([rng.uniform(0.5, 2, nS), rng.uniform(0.05, 0.3, nS), rng.uniform(3, 20, nS)])
     z = rng.normal(size=n0 * nS)
-    y0, s = R.rNNGPPredict(cm(X), y, cm(c), m, cm(X0), cm(c0), cm(nn0), cm(beta.T), cm(theta.T), 0, z)
+    y0, s = R.rNNGPPredict(cm(X), y, cm(c), m, cm(X0), cm(c0), cm(nn0), cm(beta), cm(theta), 0, z)
     assert s == 0
     out.update(pr_beta=beta, pr_theta=theta, pr_z=z, pr_y0=y0)
     bsp = rng.normal(size=(nS, p))
     normals = rng.normal(size=nS * n)
-    yr, s = R.rNNGPReplicated(cm(X), m, cm(c), 0, a[0], a[2], bsp, cm(theta.T), normals)
+    yr, s = R.rNNGPReplicated(cm(X), m, cm(c), 0, a[0], a[2], bsp, cm(theta), normals)
     assert s == 0
     out.update(rp_beta=bsp, rp_normals=normals, rp_yrep=yr)
 

@@ -1,0 +1,141 @@
+"""Model drivers on the GPU against the reference's own outputs (tests/golden) and
+the oracle: MCMC replay with host-fed streams, conjugate fit + prediction,
+response prediction, replicated data."""
+import numpy as np
+import pytest
+
+from conftest import cm, xorder
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9  # FP64 mode; the chain's arithmetic differs from the reference's only in rounding
+
+
+def mcmc_args(g, model):
+    t = f"mc{model}"
+    return dict(y=g["mc_y"], X=g["mc_X"], m=10, coords=g["mc_coords"], cov_model=model, nn_indx=g["mc_nnIndx"],
+                nn_indx_lu=g["mc_lu"], sigma_sq_IG=[2, 1], tau_sq_IG=[2, 0.1], phi_unif=[3, 30],
+                nu_unif=[0.5, 2.5], beta_starting=[1.0, -0.5], theta_starting=g[f"{t}_theta_start"],
+                tuning=g[f"{t}_tuning"], n_samples=150, normals=g[f"{t}_normals"], unifs=g[f"{t}_unifs"], n_rep=5,
+                rep_indx=g[f"{t}_repindx"])
+
+
+@pytest.mark.parametrize("model", [0, 2])
+def test_rNNGP_replays_reference_chain(sp, golden, model):
+    r = sp.rNNGP(**mcmc_args(golden, model), precision="fp64")
+    t = f"mc{model}"
+    th, gth = r["p.theta.samples"], golden[f"{t}_theta"]
+    # identical accept/reject sequence: the chain moves at exactly the same iterations
+    moved = np.any(np.diff(th, axis=1) != 0, axis=0)
+    gmoved = np.any(np.diff(gth, axis=1) != 0, axis=0)
+    assert np.array_equal(moved, gmoved)
+    assert np.max(np.abs(th - gth) / np.abs(gth)) <= TOL
+    assert np.max(np.abs(r["p.beta.samples"] - golden[f"{t}_beta"])) <= 1e-8
+    assert np.max(np.abs(r["y.rep.samples"] - golden[f"{t}_rep"])) <= 1e-8
+
+
+@pytest.mark.parametrize("model", [0, 2])
+def test_rNNGP_fp32r_same_decisions(sp, golden, model):
+    a = mcmc_args(golden, model)
+    r = sp.rNNGP(**a, precision="fp32r")
+    t = f"mc{model}"
+    th, gth = r["p.theta.samples"], golden[f"{t}_theta"]
+    moved = np.any(np.diff(th, axis=1) != 0, axis=0)
+    gmoved = np.any(np.diff(gth, axis=1) != 0, axis=0)
+    # log-target error <= 1e-6 relative: decisions agree except on knife-edge uniforms
+    assert np.mean(moved == gmoved) >= 0.97
+    assert np.allclose(th.mean(axis=1), gth.mean(axis=1), rtol=0.05)
+
+
+def test_rNNGP_matches_oracle_longer(sp, orc):
+    rng = np.random.default_rng(21)
+    n, m, p, nS = 1500, 15, 2, 400
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    y = X @ [1.0, -0.5] + rng.normal(size=n)
+    o = orc.mkNNIndxCB(cm(c), m)
+    normals = rng.normal(size=nS * 5 + 10)
+    unifs = rng.uniform(size=nS + 2)
+    args = (y, cm(X), m, cm(c), 0, o[0], o[2], [2, 1], [2, 0.1], [3, 30], [0, 0], [1.0, -0.5], [1.0, 0.2, 6.0],
+            [0.1, 0.1, 0.4], nS, normals, unifs)
+    ro = orc.rNNGP(*args)
+    rg = sp.rNNGP(y, X, m, c, "exponential", o[0], o[2], [2, 1], [2, 0.1], [3, 30], None, [1.0, -0.5],
+                  [1.0, 0.2, 6.0], [0.1, 0.1, 0.4], nS, normals, unifs)
+    assert rg["accept"] == ro["accept"]
+    assert np.max(np.abs(rg["p.theta.samples"] - ro["theta"]) / ro["theta"]) <= TOL
+
+
+def test_rNNGP_zero_tuning_consumes_no_draw(sp, orc):
+    rng = np.random.default_rng(22)
+    n, m, nS = 400, 10, 60
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    y = X @ [1.0, -0.5] + rng.normal(size=n)
+    o = orc.mkNNIndxCB(cm(c), m)
+    normals = rng.normal(size=nS * 5)
+    unifs = rng.uniform(size=nS)
+    tun = [0.0, 0.1, 0.3]  # sigma.sq fixed: rnorm(mu, 0) returns mu without a draw
+    ro = orc.rNNGP(y, cm(X), m, cm(c), 0, o[0], o[2], [2, 1], [2, 0.1], [3, 30], [0, 0], [1.0, -0.5],
+                   [1.0, 0.2, 6.0], tun, nS, normals, unifs)
+    rg = sp.rNNGP(y, X, m, c, 0, o[0], o[2], [2, 1], [2, 0.1], [3, 30], None, [1.0, -0.5], [1.0, 0.2, 6.0], tun,
+                  nS, normals, unifs)
+    assert np.max(np.abs(rg["p.theta.samples"] - ro["theta"]) / ro["theta"]) <= TOL
+    assert np.all(rg["p.theta.samples"][0] == 1.0)
+
+
+def test_rNNGP_stream_too_short_raises(sp, golden):
+    a = mcmc_args(golden, 0)
+    a["normals"] = a["normals"][:50]
+    with pytest.raises(sp.NNGPError) as e:
+        sp.rNNGP(**a)
+    assert e.value.status == 5
+
+
+@pytest.mark.parametrize("model", [0, 2])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32r", 1e-5)])
+def test_cNNGP_matches_reference(sp, golden, model, precision, tol):
+    g = golden
+    t = f"cj{model}"
+    r = sp.cNNGP(g["mc_y"], g["mc_X"], g["mc_coords"], g[f"{t}_theta_alpha"].T, g["mc_nnIndx"], g["mc_lu"], g["cj_X0"],
+                 g["cj_coords0"], g["cj_nnIndx0"], 10, [2.0, 1.0], model, precision=precision)
+    for k, ref in (("beta.hat", g[f"{t}_beta"]), ("ab", g[f"{t}_ab"]), ("bb", g[f"{t}_bb"]),
+                   ("y.0.hat", g[f"{t}_y0"]), ("y.0.hat.var", g[f"{t}_y0var"])):
+        assert np.max(np.abs(r[k] - ref)) <= tol * max(1.0, np.max(np.abs(ref))), k
+    p = 2
+    for j in range(r["bB.inv"].shape[1]):
+        low = np.tril(r["bB.inv"][:, j].reshape(p, p).T)
+        ref = np.tril(g[f"{t}_bBInv"][:, j].reshape(p, p).T)
+        assert np.max(np.abs(low - ref)) <= tol * max(1.0, np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32r", 1e-5)])
+def test_rNNGPPredict_matches_reference(sp, golden, precision, tol):
+    g = golden
+    r = sp.rNNGPPredict(g["mc_X"], g["mc_y"], g["mc_coords"], 10, g["cj_X0"], g["cj_coords0"], g["cj_nnIndx0"],
+                        g["pr_beta"], g["pr_theta"], 0, g["pr_z"], precision=precision)
+    assert np.max(np.abs(r["p.y.0"] - g["pr_y0"])) <= tol * max(1.0, np.max(np.abs(g["pr_y0"])))
+
+
+def test_rNNGPReplicated_matches_reference(sp, golden):
+    g = golden
+    r = sp.rNNGPReplicated(g["mc_X"], 10, g["mc_coords"], 0, g["mc_nnIndx"], g["mc_lu"], g["rp_beta"],
+                           g["pr_theta"], g["rp_normals"])
+    assert np.max(np.abs(r["y.rep.samples"] - g["rp_yrep"])) <= 1e-8
+
+
+def test_cNNGP_many_grid_points_match_oracle(sp, orc):
+    rng = np.random.default_rng(31)
+    n, m, p, n0 = 3000, 15, 3, 300
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=(n, p - 1))])
+    y = X @ np.arange(1, p + 1) + rng.normal(size=n)
+    c0 = rng.uniform(size=(n0, 2))
+    X0 = np.column_stack([np.ones(n0), rng.normal(size=(n0, p - 1))])
+    o = orc.mkNNIndxCB(cm(c), m)
+    nn0, _ = orc.nn2(c, c0, m)
+    ta = np.array([[phi, a] for phi in np.linspace(3, 30, 8) for a in np.linspace(0.05, 2, 5)]).T
+    ro = orc.cNNGP(y, cm(X), cm(c), ta.T.reshape(-1), o[0], o[2], cm(X0), cm(c0), cm(nn0), m, [2, 1], 0)
+    rg = sp.cNNGP(y, X, c, ta, o[0], o[2], X0, c0, nn0, m, [2, 1], "exponential")
+    assert np.max(np.abs(rg["beta.hat"] - ro["beta"])) <= 1e-9
+    assert np.max(np.abs(rg["y.0.hat"] - ro["y0"])) <= 1e-9
+    assert np.max(np.abs(rg["y.0.hat.var"] - ro["y0var"]) / ro["y0var"]) <= 1e-9

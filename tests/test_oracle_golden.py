@@ -82,10 +82,10 @@ def test_conjugate(orc, golden, model):
 def test_predict_and_replicates(orc, golden):
     g = golden
     y0, st = orc.rNNGPPredict(cm(g["mc_X"]), g["mc_y"], cm(g["mc_coords"]), 10, cm(g["cj_X0"]), cm(g["cj_coords0"]),
-                              cm(g["cj_nnIndx0"]), cm(g["pr_beta"].T), cm(g["pr_theta"].T), 0, g["pr_z"])
+                              cm(g["cj_nnIndx0"]), cm(g["pr_beta"]), cm(g["pr_theta"]), 0, g["pr_z"])
     assert st == 0 and np.max(np.abs(y0 - g["pr_y0"])) <= 1e-10
     yr, st = orc.rNNGPReplicated(cm(g["mc_X"]), 10, cm(g["mc_coords"]), 0, g["mc_nnIndx"], g["mc_lu"], g["rp_beta"],
-                                 cm(g["pr_theta"].T), g["rp_normals"])
+                                 cm(g["pr_theta"]), g["rp_normals"])
     assert st == 0 and np.max(np.abs(yr - g["rp_yrep"])) <= 1e-9
 
 
