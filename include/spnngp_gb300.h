@@ -202,6 +202,25 @@ int nngp_measure_peak(nngp_ctx *ctx, int fp64, double *flops_per_s);
 int nngp_set_kernel_timing(nngp_ctx *ctx, int on);
 int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches);
 
+/* No counterpart in the reference.  The FP64 fused likelihood pass of
+ * nngp_loglik_gram_dev for callers that cannot allocate device memory when they
+ * need it (a host whose allocator owns all device memory, a serving process that
+ * reserves HBM up front and forbids allocation on its request path, a loop that
+ * must not hit the allocator's implicit synchronisation).  It calls no
+ * cudaMalloc / cudaFree or other allocating routine: its working memory is one
+ * statically sized __device__ array in this library (about 5.3 MB, held by every
+ * GPU that loads the library until the process exits).  Limits: n <= 65536,
+ * m <= 32, nv <= 8; larger requests return NNGP_ERR_ARG with a message in errbuf.
+ * stream is a cudaStream_t (NULL = legacy default stream); every array is a
+ * device pointer except theta (host) and errbuf (host, may be NULL).  The first
+ * call on a device looks up the array's address and configures the kernel, so
+ * make it before any stream capture.  All calls share the array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller. */
+int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, const double *coords,
+                             const int *nnIndx, const int *nnIndxLU, const double *V, int covModel,
+                             const double *theta, double *logDet, double *gram, char *errbuf,
+                             int errlen);
+
 #ifdef __cplusplus
 }
 #endif
