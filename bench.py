@@ -82,6 +82,9 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0:  # sampling must cover the timed region
+                time.sleep(0.05)
         except Exception:
             self.proc = None
         return self
@@ -133,6 +136,264 @@ def cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, n):
     r = Xcm[:n] * 1.0 + Xcm[n:] * -0.5 - y
     q = orc.Q(B, F, r, r, nn, lu, threads=threads)
     return -0.5 * (ld + q)
+
+
+def nngp_draw(sp, ctx, c, nn, lu, m, model, theta, rng):
+    """One draw of w ~ NNGP(0, sigma^2 R(phi[, nu])) on the given neighbor sets: B and F from
+    the library's FP64 updateBF (tau^2 = 0, a 1e-6 nugget for the gaussian model), then the
+    sparse unit lower-triangular solve (I - B) w = F^(1/2) z."""
+    import scipy.sparse as sps
+    from scipy.sparse.linalg import spsolve_triangular
+
+    n = len(c)
+    tau = 1e-6 if model == 3 else 0.0
+    B, F, _ = sp.updateBF(c, nn, lu, m, model, [theta[0], tau, theta[2]] + list(theta[3:]), ctx=ctx)
+    rows = np.repeat(np.arange(n), lu[n:])
+    L = sps.csr_matrix((-B, (rows, nn)), shape=(n, n)) + sps.identity(n, format="csr")
+    return spsolve_triangular(L.tocsr(), np.sqrt(F) * rng.normal(size=n), lower=True, unit_diagonal=True)
+
+
+def section_mcmc_batch(sp, ctx, dev, iters, n_inst=256, seed=77):
+    """Uneven multi-instance rNNGP: n_inst independent datasets, n log-uniform in [500, 50000],
+    m cycling 10/15/20, cov.model cycling exponential/spherical/gaussian/matern (nu 0.5/1.5/2.5,
+    held fixed: tuning 0 on nu), priors sigma.sq IG(2,1), tau.sq IG(2,0.1), phi Unif(3,30).
+    One step = one Metropolis-within-Gibbs iteration of every chain."""
+    import ctypes as C
+
+    import torch
+    from spnngp_gb300._lib import MCMCProblem
+
+    rng = np.random.default_rng(seed)
+    models = ["exponential", "spherical", "gaussian", "matern"]
+    probs = (MCMCProblem * n_inst)()
+    keep, total_n, ns = [], 0, []
+    t0 = time.perf_counter()
+    for k in range(n_inst):
+        n = int(np.exp(rng.uniform(np.log(500), np.log(50000))))
+        m = (10, 15, 20)[k % 3]
+        model = k % 4
+        nu = (0.5, 1.5, 2.5)[(k // 4) % 3]
+        c = rng.uniform(size=(n, 2))
+        c = c[np.argsort(c[:, 0], kind="stable")]
+        X = np.column_stack([np.ones(n), rng.normal(size=n)])
+        nb = sp.mkNNIndxCB(c, m, ctx=ctx)
+        nn, lu = nb["nnIndx"], nb["nnIndxLU"]
+        theta = [1.0, 0.1, 6.0] + ([nu] if model == 2 else [])
+        w = nngp_draw(sp, ctx, c, nn, lu, m, model, theta, rng)
+        y = X @ np.array([1.0, -0.5]) + w + rng.normal(scale=np.sqrt(0.1), size=n)
+        nT = 4 if model == 2 else 3
+        tun = [0.1, 0.1, 0.5, 0.0][:nT]
+        nNorm = iters * (2 + 3) + 8
+        dev_arrays = {
+            "y": torch.from_numpy(y).to(dev), "X": torch.from_numpy(np.ascontiguousarray(X.T).reshape(-1)).to(dev),
+            "coords": torch.from_numpy(np.ascontiguousarray(c.T).reshape(-1)).to(dev),
+            "nnIndx": torch.from_numpy(nn).to(dev), "nnIndxLU": torch.from_numpy(lu).to(dev),
+            "normals": torch.from_numpy(rng.normal(size=nNorm)).to(dev),
+            "unifs": torch.from_numpy(rng.uniform(size=iters + 1)).to(dev),
+            "betaSamples": torch.zeros(2 * iters, dtype=torch.float64, device=dev),
+            "thetaSamples": torch.zeros(nT * iters, dtype=torch.float64, device=dev)}
+        host_arrays = {"sigmaSqIG": np.array([2.0, 1.0]), "tauSqIG": np.array([2.0, 0.1]),
+                       "phiUnif": np.array([3.0, 30.0]), "nuUnif": np.array([0.1, 3.0]),
+                       "betaStarting": np.array([1.0, -0.5]),
+                       "thetaStarting": np.array(theta + [0.0] * (4 - nT)),
+                       "tuning": np.array(tun + [0.0] * (4 - nT))}
+        P = probs[k]
+        P.n, P.m, P.covModel, P.nSamples = n, m, model, iters
+        for name, t in dev_arrays.items():
+            setattr(P, name, t.data_ptr())
+        for name, a in host_arrays.items():
+            setattr(P, name, a.ctypes.data)
+        P.nNormals, P.nUnifs = nNorm, iters + 1
+        keep.append((dev_arrays, host_arrays, (c, X, y, nn, lu)))
+        total_n += n
+        ns.append(n)
+    gen_s = time.perf_counter() - t0
+
+    def run(resident, n_iter):
+        for P in probs:
+            P.nSamples = n_iter
+        ctx.call("nngp_rNNGP_batch", n_inst, C.cast(probs, C.c_void_p), 2, 1, resident)
+
+    run(1, 3)  # warm-up: plans, graph capture, allocator pool
+    torch.cuda.synchronize()
+    ctx.reset_launches()
+    t0 = time.perf_counter()
+    run(1, iters)
+    dt = time.perf_counter() - t0
+    launches = ctx.launches
+    acc = [P.nAccept for P in probs]
+    # the same chains through the host-memory form of the call (uploads and sample readback inside)
+    hprobs = (MCMCProblem * n_inst)()
+    hkeep = []
+    for k in range(n_inst):
+        dev_arrays, host_arrays, (c, X, y, nn, lu) = keep[k]
+        src = probs[k]
+        H = hprobs[k]
+        C.memmove(C.addressof(H), C.addressof(src), C.sizeof(MCMCProblem))
+        nT = 4 if src.covModel == 2 else 3
+        ha = {"y": y, "X": np.ascontiguousarray(X.T).reshape(-1), "coords": np.ascontiguousarray(c.T).reshape(-1),
+              "nnIndx": nn, "nnIndxLU": lu, "normals": dev_arrays["normals"].cpu().numpy(),
+              "unifs": dev_arrays["unifs"].cpu().numpy(), "betaSamples": np.zeros(2 * iters),
+              "thetaSamples": np.zeros(nT * iters)}
+        for name, a in ha.items():
+            setattr(H, name, a.ctypes.data)
+        hkeep.append(ha)
+    h2d = sum(a.nbytes for ha in hkeep for nm, a in ha.items() if nm not in ("betaSamples", "thetaSamples"))
+    d2h = sum(ha["betaSamples"].nbytes + ha["thetaSamples"].nbytes for ha in hkeep)
+    t0 = time.perf_counter()
+    ctx.call("nngp_rNNGP_batch", n_inst, C.cast(hprobs, C.c_void_p), 2, 1, 0)
+    e2e_dt = time.perf_counter() - t0
+    same = all(hprobs[k].nAccept == acc[k] for k in range(n_inst))
+    return {
+        "workload": f"{n_inst} independent response-model chains, n log-uniform [500, 50000] (total {total_n}), "
+                    "m cycling 10/15/20, cov.model cycling exponential/spherical/gaussian/matern(nu 0.5/1.5/2.5 "
+                    "fixed), y = X beta + w + eps with w an NNGP draw, FP32R",
+        "iterations": iters, "seconds": dt, "iterations_per_s": iters / dt, "ms_per_iteration": dt * 1e3 / iters,
+        "solves_per_s": total_n * iters / dt, "gpu_launches": int(launches),
+        "launches_per_iteration": launches / iters,
+        "mean_accept_rate": float(np.mean(acc)) / iters,
+        "e2e": {"seconds": e2e_dt, "iterations_per_s": iters / e2e_dt, "h2d_bytes": int(h2d), "d2h_bytes": int(d2h),
+                "same_accept_counts_as_resident": same},
+        "data_generation_s": gen_s,
+        "iterations_note": "the timed call includes plan building and graph capture; 5000 iterations scale "
+                           "linearly from this",
+    }
+
+
+def clustered_coords(rng, n, blobs=20, sd=0.03, uniform_frac=0.2):
+    """Mixture of Gaussian blobs (clipped to the unit square) plus a uniform share."""
+    nu = int(round(uniform_frac * n))
+    centers = rng.uniform(0.1, 0.9, size=(blobs, 2))
+    lab = rng.integers(0, blobs, size=n - nu)
+    c = np.vstack([np.clip(centers[lab] + rng.normal(scale=sd, size=(n - nu, 2)), 0.0, 1.0),
+                   rng.uniform(size=(nu, 2))])
+    return c[rng.permutation(n)]
+
+
+def section_conj_sweep(sp, ctx, orc=None, n=200_000, seed=91):
+    """Batched spConjNNGP: n clustered locations (20 blobs, sd 0.03, plus 20% uniform), p = 3
+    covariates N(0,1), y = X beta + w + eps with w an NNGP draw at phi = 10, sigma^2 = 1 and
+    tau^2 = 0.2; grid 50 phi in [3,30] x 20 alpha in [0.05,2]; 5 uneven random folds; m = 15."""
+    from spnngp_gb300.api import spConjNNGP
+
+    rng = np.random.default_rng(seed)
+    c = clustered_coords(rng, n)
+    X = np.column_stack([np.ones(n), rng.normal(size=n), rng.normal(size=n)])
+    o = np.argsort(c[:, 0], kind="stable")
+    co = c[o]
+    nb = sp.mkNNIndxCB(co, M, ctx=ctx)
+    w = np.empty(n)
+    w[o] = nngp_draw(sp, ctx, co, nb["nnIndx"], nb["nnIndxLU"], M, 0, [1.0, 0.0, 10.0], rng)
+    y = X @ np.array([1.0, 0.5, -0.5]) + w + rng.normal(scale=np.sqrt(0.2), size=n)
+    phis, alphas = np.linspace(3, 30, 50), np.linspace(0.05, 2, 20)
+    ta = np.array([[ph, al] for ph in phis for al in alphas])
+    perm = rng.permutation(n)
+    cuts = np.cumsum((np.array([0.12, 0.16, 0.20, 0.24, 0.28]) * n).astype(int))[:-1]
+    folds = np.split(perm, cuts)  # uneven folds, indices in the NNGP (x) order
+    g = len(ta)
+    solves = sum((n - len(f)) * g + len(f) * g for f in folds) + n
+    res = {}
+    for prec in ("fp32r", "fp64"):
+        t0 = time.perf_counter()
+        r = spConjNNGP(y, X, c, n_neighbors=M, theta_alpha=ta, sigma_sq_IG=[2.0, 1.0],
+                              cov_model="exponential", k_fold=5, folds=folds, precision=prec, ctx=ctx,
+                              return_neighbor_info=False)
+        res[prec] = (time.perf_counter() - t0, r)
+    t32, r32 = res["fp32r"]
+    t64, r64 = res["fp64"]
+    s32, s64 = r32["k.fold.scores"][:, 2:], r64["k.fold.scores"][:, 2:]
+    out = {
+        "workload": f"spConjNNGP k-fold sweep: n={n} clustered (20 blobs sd 0.03 + 20% uniform), p=3, "
+                    f"{g}-point (phi, alpha) grid, 5 uneven folds, m={M}, exponential, CRPS selection",
+        "seconds_fp32r": t32, "seconds_fp64": t64, "solves": int(solves),
+        "solves_per_s_fp32r": solves / t32, "solves_per_s_fp64": solves / t64,
+        "selected_fp32r": r32["theta.alpha"], "selected_fp64": r64["theta.alpha"],
+        "same_selection": r32["theta.alpha"] == r64["theta.alpha"],
+        "score_max_rel_err_fp32r_vs_fp64": float(np.max(np.abs(s32 - s64) / np.abs(s64))),
+        "note": "timed through the public spConjNNGP call (host data in, per-fold neighbor searches, "
+                "one fused launch over all folds x grid points, device scoring, final fit)",
+    }
+    if orc is not None:
+        # the oracle's C port of cNNGP on one fold at 4 grid points, all host threads
+        keep = np.ones(n, bool)
+        keep[folds[0]] = False  # fold indices are positions in the x order
+        cm_, ym, Xm = co[keep], y[o][keep], X[o][keep]
+        nbm = orc.mkNNIndxCB(np.ascontiguousarray(cm_.T).reshape(-1), M, threads=os.cpu_count() or 1)
+        thr = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        orc.cNNGP(ym, np.ascontiguousarray(Xm.T).reshape(-1), np.ascontiguousarray(cm_.T).reshape(-1),
+                  ta[:4].reshape(-1), nbm[0], nbm[2], None, None, None, M, [2.0, 1.0], 0, threads=thr)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(ym) * 4 / dt, "unit": "solves/s", "cores": thr, "kind": "port",
+                               "sample": f"oracle cNNGP (port of src/cNNGP.cpp:73-358) on one fold "
+                                         f"(n={len(ym)}) at 4 grid points, no prediction"}
+    return out
+
+
+def section_serving(sp, ctx, rates=(10, 50, 100, 200, 500), seed=55, max_requests=200, pool=32):
+    """Serving: Poisson streams of spConjNNGP fit + predict requests, n log-uniform in [1e3, 5e5],
+    prediction sets of U[1e3, 1e5] uniform points, m = 15, exponential, (phi, alpha) from the
+    50 x 20 grid, HBM budget 150 GB; the continuous-batching server against the plain
+    per-request form on the same arrival times."""
+    from spnngp_gb300 import serving as S
+
+    rng = np.random.default_rng(seed)
+    datasets = []
+    for k in range(pool):
+        n = int(np.exp(rng.uniform(np.log(1e3), np.log(5e5))))
+        c = rng.uniform(size=(n, 2))
+        X = np.column_stack([np.ones(n), rng.normal(size=n)])
+        y = X @ np.array([1.0, -0.5]) + np.sin(5 * c[:, 0]) * np.cos(3 * c[:, 1]) + rng.normal(scale=0.3, size=n)
+        datasets.append((c, X, y))
+    preds = []
+    for k in range(pool):
+        n0 = int(rng.uniform(1e3, 1e5))
+        preds.append((rng.uniform(size=(n0, 2)), np.column_stack([np.ones(n0), rng.normal(size=n0)])))
+    phis, alphas = np.linspace(3, 30, 50), np.linspace(0.05, 2, 20)
+
+    def stream(rate, count):
+        t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+        reqs = []
+        for k in range(count):
+            di, pi = int(rng.integers(pool)), int(rng.integers(pool))
+            c, X, y = datasets[di]
+            c0, X0 = preds[pi]
+            reqs.append(S.ConjRequest(c, X, y, c0, X0, float(rng.choice(phis)), float(rng.choice(alphas)),
+                                      dataset=di, rid=k, arrival=float(t[k])))
+        return reqs
+
+    # warm-up: every dataset resident once, kernels loaded
+    srv = S.ConjServer(m=M, precision="fp32r", hbm_budget=150e9, ctx=ctx)
+    S.serve(srv, stream(1000.0, pool), realtime=False)
+    for d in range(pool):
+        c, X, y = datasets[d]
+        c0, X0 = preds[d]
+        srv.submit(S.ConjRequest(c, X, y, c0, X0, 10.0, 0.5, dataset=d, rid=-1 - d))
+    srv.drain()
+    # accuracy of the served (FP32R) results against FP64 on a sample
+    errs = []
+    for k, r in enumerate(stream(1000.0, 6)):
+        srv.submit(r)
+        got = srv.step()[0]
+        ref = S.fit_predict_one(r, m=M, precision="fp64", ctx=ctx)
+        errs.append(max(abs(got.ab[1] - ref.ab[1]) / abs(ref.ab[1]),
+                        float(np.max(np.abs(got.y0_hat - ref.y0_hat)) / max(1.0, np.max(np.abs(ref.y0_hat))))))
+    rows = []
+    for rate in rates:
+        count = int(min(max_requests, max(40, rate * 2)))
+        reqs = stream(rate, count)
+        a = S.serve(srv, reqs)
+        b = S.serve_per_request(reqs, m=M, precision="fp32r", ctx=ctx)
+        same = all(np.array_equal(x.y0_hat, y.y0_hat) for x, y in
+                   zip(sorted(a["results"], key=lambda r: r.rid), sorted(b["results"], key=lambda r: r.rid)))
+        rows.append({"rate_rps": rate, "requests": count,
+                     "server": {k: a[k] for k in ("throughput_rps", "p50_s", "p99_s", "mean_batch", "failed")},
+                     "per_request": {k: b[k] for k in ("throughput_rps", "p50_s", "p99_s", "failed")},
+                     "identical_outputs": same})
+    return {"workload": f"Poisson streams of conjugate fit+predict requests over {pool} datasets (n log-U[1e3,5e5]) "
+                        f"and {pool} prediction sets (n0 U[1e3,1e5]), m={M}, exponential, FP32R, HBM budget 150 GB",
+            "rates": rows, "max_rel_err_fp32r_vs_fp64": float(max(errs)),
+            "server_cache": dict(srv.stats)}
 
 
 def run_reference(args):
@@ -241,12 +502,13 @@ def run_ours(args):
         ms = float(sum(e0.elapsed_time(e1) for e0, e1 in ev))
         return ms / steps, kms.value / max(kn.value, 1), launches
 
+    # the clock sampler spans every timed region (FP64 form, FP32R headline, e2e)
+    clk = ClockSampler(dev.index).__enter__()
     # FP64 form (for the >= 3x comparison and the error reference)
     ms64, kms64, _ = timed(0, max(3, args.steps // 4), 2)
     ll64 = loglik()
-    # FP32R headline, timed region under the clock sampler
-    with ClockSampler(dev.index) as clk:
-        ms32, kms32, launches = timed(1, args.steps, args.warmup)
+    # FP32R headline
+    ms32, kms32, launches = timed(1, args.steps, args.warmup)
     ll32 = loglik()
     max_ms = ms32
     if ws > 1:
@@ -275,6 +537,7 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    clk.__exit__(None, None, None)
     h2d = h_c.nbytes + h_nn.nbytes + h_lu.nbytes + h_V.nbytes
     d2h = h_ld.nbytes + h_G.nbytes
 
@@ -316,6 +579,24 @@ def run_ours(args):
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
 
+    sections = {}
+    if rank == 0 and args.sections:
+        clk2 = ClockSampler(dev.index).__enter__()
+        if "mcmc" in args.sections:
+            sections["mcmc_batch"] = section_mcmc_batch(sp, ctx, dev, args.mcmc_iters)
+        if "conj" in args.sections:
+            orc = None
+            if not args.skip_cpu:
+                from oracle.oracle import Oracle, build as build_oracle
+
+                build_oracle()
+                orc = Oracle()
+            sections["conj_sweep"] = section_conj_sweep(sp, ctx, orc)
+        if "serve" in args.sections:
+            sections["serving"] = section_serving(sp, ctx)
+        clk2.__exit__(None, None, None)
+        sections["sections_clocks"] = clk2.summary()
+
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -342,6 +623,7 @@ def run_ours(args):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
+        out.update(sections)
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -354,8 +636,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--sections", default="mcmc,conj,serve",
+                    help="comma-separated extra workloads reported beside the headline (mcmc, conj, serve), or ''")
+    ap.add_argument("--mcmc-iters", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.sections = [x for x in args.sections.split(",") if x]
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -146,6 +146,33 @@ int nngp_rNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, in
                int precision, double *betaSamples, double *thetaSamples, double *repSamples,
                int *nAccept);
 
+/* One response-model chain of a batch (the arguments of nngp_rNNGP that may
+ * differ between chains, without replicates).  nAccept is an output. */
+typedef struct nngp_mcmc_problem {
+  int n, m, covModel, nSamples;
+  const double *y, *X, *coords;
+  const int *nnIndx, *nnIndxLU;
+  const double *sigmaSqIG, *tauSqIG, *phiUnif, *nuUnif;       /* host memory, 2 each */
+  const double *betaStarting, *thetaStarting, *tuning;        /* host memory */
+  const double *normals;
+  int64_t nNormals;
+  const double *unifs;
+  int64_t nUnifs;
+  double *betaSamples, *thetaSamples;
+  int nAccept;
+} nngp_mcmc_problem;
+
+/* Independent response-model chains advanced together: each iteration runs
+ * every chain's likelihood pass in one fused launch per neighbor-count class
+ * (m <= 16, m <= 32), the whole iteration replayed as one CUDA graph.  Each
+ * chain's draws are those nngp_rNNGP gives it alone on the same streams.
+ * All chains share p.  resident != 0: y, X, coords, nnIndx, nnIndxLU,
+ * normals, unifs, betaSamples and thetaSamples are device memory; resident ==
+ * 0: host memory.  Replaces a loop of rNNGP calls (src/rNNGP.cpp:103-421) over
+ * independent data sets, as a simulation study or a model-selection sweep runs it. */
+int nngp_rNNGP_batch(nngp_ctx *ctx, int nprob, nngp_mcmc_problem *probs, int p, int precision,
+                     int resident);
+
 /* Conjugate NNGP over g parameter sets with prediction at n0 points.
  * Argument meaning follows .Call("cNNGP", ...) (R/spConjNNGP.R:336-338,
  * src/cNNGP.cpp:73-75).  Outputs betaHat p x g, ab 2 x g, bBInv p*p x g (lower
@@ -157,6 +184,34 @@ int nngp_cNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n,
                const int *nnIndx0, int g, int m, const double *sigmaSqIG, int covModel,
                int precision, double *betaHat, double *ab, double *bBInv, double *bb,
                double *y0Hat, double *y0HatVar);
+
+/* One dataset of a batched conjugate run (nngp_cNNGP_multi).  Inputs follow
+ * nngp_cNNGP; thetaAlpha is nTheta x g for this dataset.  y0True (n0, may be
+ * NULL) are held-out responses: when given, the run also scores every
+ * parameter set by CRPS and RMSPE over the n0 points as R/util.R:247-255 does
+ * (crps, rmspe: g each).  Outputs as nngp_cNNGP (y0Hat / y0HatVar may be NULL
+ * when only the scores are wanted). */
+typedef struct {
+  int n, n0, g;
+  const double *y, *X, *coords;
+  const int *nnIndx, *nnIndxLU;
+  const double *X0, *coords0;
+  const int *nnIndx0;
+  const double *thetaAlpha;
+  const double *y0True;
+  double *betaHat, *ab, *bBInv, *bb, *y0Hat, *y0HatVar, *crps, *rmspe;
+} nngp_conj_problem;
+
+/* Batched conjugate fits: every (dataset, parameter set) of every problem in
+ * one fused likelihood launch, then the p x p algebra, the prediction solves
+ * and the optional scores.  One call replaces the k-fold loop of
+ * R/spConjNNGP.R:287-358 (k calls of src/cNNGP.cpp:73-358 plus crps/rmspe),
+ * or a batch of independent fits.  All problems share p, m, sigmaSqIG and
+ * covModel.  resident != 0: every array in probs except thetaAlpha is device
+ * memory (nothing is copied); resident == 0: host memory.  thetaAlpha (nTheta x
+ * g) is always host memory. */
+int nngp_cNNGP_multi(nngp_ctx *ctx, int nprob, const nngp_conj_problem *probs, int p, int m,
+                     const double *sigmaSqIG, int covModel, int precision, int resident);
 
 /* Posterior predictive draws at q points for nSamples kept samples.  betaSamples
  * p x nSamples, thetaSamples nTheta x nSamples, z q*nSamples standard normals
@@ -189,6 +244,8 @@ int nngp_loglik_gram_dev(nngp_ctx *ctx, int n, int m, int nv, const double *coor
                          const double *theta, int precision, double *logDet, double *gram);
 int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx,
                         double *nnDist, int *nnIndxLU);
+int nngp_nn2_dev(nngp_ctx *ctx, int n, const double *coords, int n0, const double *coords0, int k,
+                 int *nnIdx, double *nnDist);
 
 /* Measurement utility, no counterpart in the reference: sustained FMA
  * throughput (FLOP/s) of the FP64 (fp64 != 0) or FP32 CUDA-core pipe, the

@@ -7,7 +7,7 @@ reference's R entry points.  Importing it does not touch the GPU; the first
 call that needs the library loads it and raises if it is missing.
 """
 from ._lib import FP32R, FP64, Context, NNGPError, default_context, lib  # noqa: F401
-from .core import (COV_MODELS, Q, cNNGP, cov_model_index, loglik_gram, mkNNIndx, mkNNIndxCB,  # noqa: F401
+from .core import (COV_MODELS, Q, cNNGP, cNNGP_multi, rNNGP_batch, cov_model_index, loglik_gram, mkNNIndx, mkNNIndxCB,  # noqa: F401
                    mkUIndx, nn2, rNNGP, rNNGPPredict, rNNGPReplicated, updateBF, updateConjBF)
 
 __version__ = "0.1.0"

@@ -56,10 +56,32 @@ _SIGNATURES = {
     "nngp_updateBF_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp, _vp]),
     "nngp_loglik_gram_dev": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp]),
     "nngp_mkNNIndxCB_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
+    "nngp_nn2_dev": (_i, [_vp, _i, _vp, _i, _vp, _i, _vp, _vp]),
     "nngp_measure_peak": (_i, [_vp, _i, _dp]),
+    "nngp_cNNGP_multi": (_i, [_vp, _i, _vp, _i, _i, _dp, _i, _i, _i]),
+    "nngp_rNNGP_batch": (_i, [_vp, _i, _vp, _i, _i, _i]),
     "nngp_set_kernel_timing": (_i, [_vp, _i]),
     "nngp_kernel_time": (_i, [_vp, _dp, C.POINTER(_i64)]),
 }
+
+
+class ConjProblem(C.Structure):
+    """nngp_conj_problem (include/spnngp_gb300.h): one dataset of a batched conjugate run."""
+
+    _fields_ = [("n", C.c_int), ("n0", C.c_int), ("g", C.c_int)] + [
+        (name, C.c_void_p) for name in ("y", "X", "coords", "nnIndx", "nnIndxLU", "X0", "coords0", "nnIndx0",
+                                        "thetaAlpha", "y0True", "betaHat", "ab", "bBInv", "bb", "y0Hat",
+                                        "y0HatVar", "crps", "rmspe")]
+
+
+class MCMCProblem(C.Structure):
+    """nngp_mcmc_problem (include/spnngp_gb300.h): one chain of a batched response-model run."""
+
+    _fields_ = [("n", C.c_int), ("m", C.c_int), ("covModel", C.c_int), ("nSamples", C.c_int)] + [
+        (name, C.c_void_p) for name in ("y", "X", "coords", "nnIndx", "nnIndxLU", "sigmaSqIG", "tauSqIG", "phiUnif",
+                                        "nuUnif", "betaStarting", "thetaStarting", "tuning", "normals")] + [
+        ("nNormals", C.c_int64), ("unifs", C.c_void_p), ("nUnifs", C.c_int64), ("betaSamples", C.c_void_p),
+        ("thetaSamples", C.c_void_p), ("nAccept", C.c_int)]
 
 
 class NNGPError(RuntimeError):

@@ -9,7 +9,7 @@ Everything numeric runs on the GB300 through the C ABI.
 Random numbers: the reference draws from R's global generator.  Here every call
 takes ``seed`` (or a ``numpy.random.Generator`` as ``rng``) and builds the
 host-fed streams in the reference's consumption order; an R binding fills the
-same streams from R's generator instead.
+same streams from R's generator (norm_rand / unif_rand, in the same order) instead.
 """
 from __future__ import annotations
 
@@ -365,6 +365,7 @@ def spConjNNGP(y, X, coords, knots=None, n_neighbors=15, theta_alpha=None, sigma
             raise ValueError(f"error: specified score.rule '{score_rule}' is not a valid option; choose from "
                              "rmspe, crps.")
         scores = np.zeros((ta.shape[0], 2))  # columns rmspe, crps
+        problems = []
         for f in range(int(k_fold)):
             if folds is not None:
                 ho = np.sort(np.asarray(folds[f]))
@@ -376,11 +377,14 @@ def spConjNNGP(y, X, coords, knots=None, n_neighbors=15, theta_alpha=None, sigma
             ch, Xh, yh = coords_o[ho], X_o[ho], y_o[ho]
             idx = (core.mkNNIndx if search_type == "brute" else core.mkNNIndxCB)(cm_, n_neighbors, ctx=ctx)
             nnh, _ = core.nn2(cm_, ch, n_neighbors, ctx=ctx)
-            out = core.cNNGP(ym, Xm, cm_, ta.T, idx["nnIndx"], idx["nnIndxLU"], Xh, ch, nnh, n_neighbors, sig_ig,
-                             cov_idx, precision=precision, ctx=ctx)
-            for j in range(ta.shape[0]):
-                scores[j, 1] += crps(yh, out["y.0.hat"][:, j], out["y.0.hat.var"][:, j])
-                scores[j, 0] += rmspe(yh, out["y.0.hat"][:, j])
+            problems.append({"y": ym, "X": Xm, "coords": cm_, "nn_indx": idx["nnIndx"], "nn_indx_lu": idx["nnIndxLU"],
+                             "theta_alpha": ta.T, "X0": Xh, "coords0": ch, "nn_indx0": nnh, "y0_true": yh})
+        # every fold x every parameter set in one fused launch, scored on the device
+        outs = core.cNNGP_multi(problems, n_neighbors, sig_ig, cov_idx, precision=precision, want_pred=False,
+                                ctx=ctx)
+        for o in outs:
+            scores[:, 1] += o["crps"]
+            scores[:, 0] += o["rmspe"]
         scores /= int(k_fold)
         col = 1 if score_rule == "crps" else 0
         best = int(np.argmin(scores[:, col]))

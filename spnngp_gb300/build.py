@@ -1,8 +1,9 @@
 """Builds libspnngp_gb300.so in-tree from csrc/*.cu for sm_103a.
 
-Every translation unit is compiled in parallel (the B/F kernel instantiations
-are split across files for that reason), then linked into one shared library
-with the CUDA runtime linked statically.  Objects go to ``_build/`` next to the
+Every translation unit is compiled in parallel, then linked into one shared
+library with the CUDA runtime linked statically.  nngp_bf_inst.cu is compiled
+once per B/F kernel variant (neighbor bound x precision x correlation code) so
+the heavy kernel instantiations spread over all cores.  Objects go to ``_build/`` next to the
 sources; the library lands next to this file.
 """
 from __future__ import annotations
@@ -22,6 +23,13 @@ LIB = os.path.join(HERE, "libspnngp_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-diag-suppress", "177"]
+
+
+# source -> [(object suffix, defines)]: sources compiled once per variant
+VARIANTS = {
+    "nngp_bf_inst.cu": [(f"_m{m}_{'f' if r else 'd'}_c{c}", [f"-DBF_M={m}", f"-DBF_R32={r}", f"-DBF_COV={c}"])
+                        for m in (16, 32) for r in (1, 0) for c in (0, 1, 2, 3, 4)],
+}
 
 
 def _nvcc() -> str:
@@ -55,14 +63,22 @@ def build(verbose: bool = False, extra: list[str] | None = None, force: bool = F
     jobs = []
     objs = []
     for src in sources:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        objs.append(obj)
-        if force or _stale(obj, [src, *headers]):
-            jobs.append((src, obj))
+        base = os.path.basename(src)[:-3]
+        for suffix, defs in VARIANTS.get(os.path.basename(src), [("", [])]):
+            obj = os.path.join(BUILD, base + suffix + ".o")
+            objs.append(obj)
+            if force or _stale(obj, [src, *headers]):
+                jobs.append((src, obj, defs))
+    # stale objects of sources or variants that no longer exist must not be linked
+    for old in glob.glob(os.path.join(BUILD, "*.o")):
+        if old not in objs:
+            os.remove(old)
     if jobs:
         workers = max(1, min(len(jobs), os.cpu_count() or 4))
+        # heaviest first: the FP32R and general-model variants take longest
+        jobs.sort(key=lambda j: ("_f_" not in j[1], "_c4" not in j[1], "_m32" not in j[1]))
         with cf.ThreadPoolExecutor(workers) as ex:
-            futs = [ex.submit(_compile, nvcc, s, o, extra) for s, o in jobs]
+            futs = [ex.submit(_compile, nvcc, s, o, extra + d) for s, o, d in jobs]
             for f in cf.as_completed(futs):
                 src, rc, log = f.result()
                 if verbose or rc != 0:

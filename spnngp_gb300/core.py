@@ -8,11 +8,12 @@ column-major flat vector the .Call layer receives.
 """
 from __future__ import annotations
 
+import ctypes as C
 import time
 
 import numpy as np
 
-from ._lib import FP32R, FP64, Context, NNGPError, default_context, dptr, f64, i32, iptr, n_indx
+from ._lib import FP32R, FP64, ConjProblem, Context, MCMCProblem, NNGPError, default_context, dptr, f64, i32, iptr, n_indx
 
 COV_MODELS = ("exponential", "spherical", "matern", "gaussian")  # R/spNNGP.R:172
 
@@ -301,5 +302,115 @@ def rNNGPReplicated(X, m: int, coords, cov_model, nn_indx, nn_indx_lu, beta, the
     return {"y.rep.samples": yr.reshape(nS, n).T}
 
 
+def cNNGP_multi(problems, m: int, sigma_sq_IG, cov_model, precision="fp64", want_pred=True,
+                ctx: Context | None = None) -> list:
+    """Batched conjugate fits (nngp_cNNGP_multi): every (problem, parameter set) in one fused
+    launch.  Each problem is a dict with y, X (n x p), coords (n x 2), nn_indx, nn_indx_lu,
+    theta_alpha (nTheta x g) and optionally X0, coords0, nn_indx0 (n0 x m) and y0_true (held-out
+    responses: the problem is then scored by CRPS and RMSPE per parameter set, R/util.R:247-255).
+    Returns one dict per problem with beta.hat, ab, bB.inv, bb[, y.0.hat, y.0.hat.var][, crps, rmspe]."""
+    model = cov_model_index(cov_model)
+    nTheta = 3 if model == 2 else 2
+    keep = []  # arrays must outlive the call
+    structs = (ConjProblem * len(problems))()
+    outs = []
+    p = None
+    for k, P in enumerate(problems):
+        y = f64(P["y"])
+        n = len(y)
+        Xa = np.asarray(P["X"], np.float64)
+        Xa = Xa[:, None] if Xa.ndim == 1 else Xa
+        p = Xa.shape[1] if p is None else p
+        Xc = f64(Xa.T.reshape(-1))
+        c = coords_cm(P["coords"])
+        ta = np.asarray(P["theta_alpha"], np.float64)
+        ta = f64(ta.T.reshape(-1)) if ta.ndim == 2 else f64(ta)
+        g = len(ta) // nTheta
+        nn, lu = i32(P["nn_indx"]), i32(P["nn_indx_lu"])
+        o = {"beta.hat": np.zeros(p * g), "ab": np.zeros(2 * g), "bB.inv": np.zeros(p * p * g), "bb": np.zeros(p * g)}
+        st = structs[k]
+        st.n, st.g = n, g
+        st.y, st.X, st.coords, st.nnIndx, st.nnIndxLU, st.thetaAlpha = (a.ctypes.data for a in (y, Xc, c, nn, lu, ta))
+        keep += [y, Xc, c, nn, lu, ta]
+        if P.get("coords0") is not None and len(P["coords0"]):
+            c0 = coords_cm(P["coords0"])
+            n0 = len(c0) // 2
+            X0 = np.asarray(P["X0"], np.float64)
+            X0c = f64((X0[:, None] if X0.ndim == 1 else X0).T.reshape(-1))
+            nn0 = np.asarray(P["nn_indx0"])
+            nn0 = i32(nn0.T.reshape(-1)) if nn0.ndim == 2 else i32(nn0)
+            st.n0 = n0
+            st.X0, st.coords0, st.nnIndx0 = X0c.ctypes.data, c0.ctypes.data, nn0.ctypes.data
+            keep += [X0c, c0, nn0]
+            if want_pred:
+                o["y.0.hat"], o["y.0.hat.var"] = np.zeros(n0 * g), np.zeros(n0 * g)
+                st.y0Hat, st.y0HatVar = o["y.0.hat"].ctypes.data, o["y.0.hat.var"].ctypes.data
+            if P.get("y0_true") is not None:
+                yt = f64(P["y0_true"])
+                keep.append(yt)
+                st.y0True = yt.ctypes.data
+                o["crps"], o["rmspe"] = np.zeros(g), np.zeros(g)
+                st.crps, st.rmspe = o["crps"].ctypes.data, o["rmspe"].ctypes.data
+        st.betaHat, st.ab, st.bBInv, st.bb = (o[k2].ctypes.data for k2 in ("beta.hat", "ab", "bB.inv", "bb"))
+        outs.append((o, n, g, st.n0))
+    _ctx(ctx).call("nngp_cNNGP_multi", len(problems), C.cast(structs, C.c_void_p), p, m, dptr(f64(sigma_sq_IG)),
+                   model, precision_code(precision), 0)
+    res = []
+    for o, n, g, n0 in outs:
+        r = {"beta.hat": o["beta.hat"].reshape(g, p).T, "ab": o["ab"].reshape(g, 2).T,
+             "bB.inv": o["bB.inv"].reshape(g, p * p).T, "bb": o["bb"].reshape(g, p).T}
+        if "y.0.hat" in o:
+            r["y.0.hat"] = o["y.0.hat"].reshape(g, n0).T
+            r["y.0.hat.var"] = o["y.0.hat.var"].reshape(g, n0).T
+        if "crps" in o:
+            r["crps"], r["rmspe"] = o["crps"], o["rmspe"]
+        res.append(r)
+    return res
+
+
+def rNNGP_batch(chains, precision="fp64", ctx: Context | None = None) -> list:
+    """Independent response-model chains advanced together (nngp_rNNGP_batch).  Each chain is a dict
+    with the arguments of rNNGP that may differ between chains (y, X, coords, nn_indx, nn_indx_lu, m,
+    cov_model, sigma_sq_IG, tau_sq_IG, phi_unif[, nu_unif], beta_starting, theta_starting, tuning,
+    n_samples, normals, unifs); all chains share p.  No replicate draws.  Returns one dict per chain with
+    p.beta.samples, p.theta.samples and accept -- each identical to what rNNGP gives that chain alone."""
+    structs = (MCMCProblem * len(chains))()
+    keep, outs = [], []
+    p = None
+    for k, P in enumerate(chains):
+        y = f64(P["y"])
+        n = len(y)
+        Xa = np.asarray(P["X"], np.float64)
+        Xa = Xa[:, None] if Xa.ndim == 1 else Xa
+        if p is None:
+            p = Xa.shape[1]
+        elif Xa.shape[1] != p:
+            raise ValueError("all chains of a batch must share p")
+        model = cov_model_index(P["cov_model"])
+        nTheta = 4 if model == 2 else 3
+        nS = int(P["n_samples"])
+        arrs = {"y": y, "X": f64(Xa.T.reshape(-1)), "coords": coords_cm(P["coords"]),
+                "nnIndx": i32(P["nn_indx"]), "nnIndxLU": i32(P["nn_indx_lu"]),
+                "sigmaSqIG": f64(P["sigma_sq_IG"]), "tauSqIG": f64(P["tau_sq_IG"]), "phiUnif": f64(P["phi_unif"]),
+                "nuUnif": f64(P.get("nu_unif") if P.get("nu_unif") is not None else [0.0, 0.0]),
+                "betaStarting": f64(P["beta_starting"]),
+                "thetaStarting": f64(list(np.asarray(P["theta_starting"], np.float64).reshape(-1)[:nTheta])
+                                     + [0.0] * (4 - nTheta)),
+                "tuning": f64(list(np.asarray(P["tuning"], np.float64).reshape(-1)[:nTheta]) + [0.0] * (4 - nTheta)),
+                "normals": f64(P["normals"]), "unifs": f64(P["unifs"]),
+                "betaSamples": np.zeros(max(1, p * nS)), "thetaSamples": np.zeros(max(1, nTheta * nS))}
+        st = structs[k]
+        st.n, st.m, st.covModel, st.nSamples = n, int(P["m"]), model, nS
+        for name, a in arrs.items():
+            setattr(st, name, a.ctypes.data)
+        st.nNormals, st.nUnifs = len(arrs["normals"]), len(arrs["unifs"])
+        keep.append(arrs)
+        outs.append((arrs, nS, nTheta))
+    _ctx(ctx).call("nngp_rNNGP_batch", len(chains), C.cast(structs, C.c_void_p), p, precision_code(precision), 0)
+    return [{"p.beta.samples": a["betaSamples"][: p * nS].reshape(nS, p).T,
+             "p.theta.samples": a["thetaSamples"][: nT * nS].reshape(nS, nT).T,
+             "accept": int(structs[k].nAccept)} for k, (a, nS, nT) in enumerate(outs)]
+
+
 __all__ = ["mkNNIndxCB", "mkNNIndx", "mkUIndx", "nn2", "updateBF", "updateConjBF", "Q", "loglik_gram",
-           "rNNGP", "cNNGP", "rNNGPPredict", "rNNGPReplicated", "cov_model_index", "precision_code", "coords_cm", "NNGPError", "Context", "COV_MODELS"]
+           "rNNGP", "rNNGP_batch", "cNNGP", "cNNGP_multi", "rNNGPPredict", "rNNGPReplicated", "cov_model_index", "precision_code", "coords_cm", "NNGPError", "Context", "COV_MODELS"]

@@ -7,14 +7,6 @@
 
 namespace {
 
-__global__ void interleave_kernel(const double *__restrict__ cm, int n, double *__restrict__ xy) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    xy[2 * i] = cm[i];
-    xy[2 * i + 1] = cm[n + i];
-  }
-}
-
 // col-major n x nv -> row-major n x nv
 __global__ void to_row_major_kernel(const double *__restrict__ cm, int n, int nv, double *__restrict__ rm) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,9 +85,11 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   if (precision != NNGP_FP64 && precision != NNGP_FP32R)
     return nngp_fail(ctx, NNGP_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32R)");
   double *xy, *Vrm = nullptr;
+  float *xyf = nullptr;
   NNGP_ALLOC(ctx, xy, double, S_COORDS, 2 * (size_t)n);
-  interleave_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d_coords_cm, n, xy);
-  NNGP_LAUNCH_CHECK(ctx);
+  if (precision == NNGP_FP32R) NNGP_ALLOC(ctx, xyf, float, S_XYF, 4 * (size_t)n);
+  int st0 = nngp_prepare_coords(ctx, d_coords_cm, n, xy, xyf);
+  if (st0) return st0;
   if (mode == 1) {
     NNGP_ALLOC(ctx, Vrm, double, S_V, (size_t)n * nv);
     const long tot = (long)n * nv;
@@ -117,19 +111,22 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   d.m = m;
   d.nv = nv;
   d.xy = xy;
+  d.xyf = xyf;
   d.nnIndx = d_nnIndx;
   d.nnLU = d_nnLU;
   d.V = Vrm;
   d.B = d_B;
   d.F = d_F;
   char key[256];
-  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p", mode, precision, n, m, nv, (const void *)xy,
+  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p/%p", nngp_plan_cov(&cp, 1), mode, precision, n, m, nv, (const void *)xy,
+           (const void *)xyf,
            (const void *)d_nnIndx, (const void *)d_nnLU, (const void *)Vrm, (void *)d_B, (void *)d_F,
            (void *)d_theta, (void *)d_status);
   if (!ctx->cache_plan || ctx->cache_key != key) {
     nngp_bf_cache_release(ctx);
     BFPlan *plan = new BFPlan();
-    st = nngp_bf_plan(ctx, plan, precision, mode, nv, {d}, d_theta, {PassEval{0, 0}}, d_status);
+    st = nngp_bf_plan(ctx, plan, precision, mode, nv, {d}, d_theta, {PassEval{0, 0}}, d_status,
+                      nngp_plan_cov(&cp, 1));
     if (st) {
       nngp_bf_plan_free(ctx, plan);
       delete plan;

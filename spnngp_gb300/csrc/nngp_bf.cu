@@ -3,10 +3,11 @@
 #include "nngp_internal.h"
 
 // Host side of the B/F pass: plans (job tables), dispatch to the kernel
-// instantiations of nngp_bf_inst_*.cu, and the fixed-order reductions.  The
-// kernel itself is documented in nngp_bf_kernel.cuh.
+// instantiations of nngp_bf_inst.cu (one object per neighbor bound, precision and
+// correlation code), and the fixed-order reductions.  The kernel itself is
+// documented in nngp_bf_kernel.cuh.
 namespace nngp_bf {
-template <int M, bool R32, int MODE>
+template <int M, bool R32, int MODE, int COV>
 int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass);
 template <int M, bool R32>
 constexpr int bf_tpb() {
@@ -38,13 +39,24 @@ __global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, int ng,
 }  // namespace
 
 namespace {
+template <int MODE, int COV>
+int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
+  if (pl->mmax <= 16)
+    return fp32r ? launch_one<16, true, MODE, COV>(ctx, pl, fallback_pass)
+                 : launch_one<16, false, MODE, COV>(ctx, pl, fallback_pass);
+  return fp32r ? launch_one<32, true, MODE, COV>(ctx, pl, fallback_pass)
+               : launch_one<32, false, MODE, COV>(ctx, pl, fallback_pass);
+}
+
 template <int MODE>
 int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
-  if (pl->mmax <= 16)
-    return fp32r ? launch_one<16, true, MODE>(ctx, pl, fallback_pass)
-                 : launch_one<16, false, MODE>(ctx, pl, fallback_pass);
-  return fp32r ? launch_one<32, true, MODE>(ctx, pl, fallback_pass)
-               : launch_one<32, false, MODE>(ctx, pl, fallback_pass);
+  switch (pl->cov) {
+    case NNGP_COV_EXP: return launch_mode_c<MODE, NNGP_COV_EXP>(ctx, pl, fp32r, fallback_pass);
+    case NNGP_COV_SPH: return launch_mode_c<MODE, NNGP_COV_SPH>(ctx, pl, fp32r, fallback_pass);
+    case NNGP_COV_MAT_HALF: return launch_mode_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, fp32r, fallback_pass);
+    case NNGP_COV_GAU: return launch_mode_c<MODE, NNGP_COV_GAU>(ctx, pl, fp32r, fallback_pass);
+    default: return launch_mode_c<MODE, NNGP_COV_ANY>(ctx, pl, fp32r, fallback_pass);
+  }
 }
 
 int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
@@ -94,8 +106,9 @@ static int build_jobs(int tpb, const std::vector<BFData> &datas, const std::vect
 
 int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
                  const std::vector<BFData> &datas, const CovParams *d_thetas,
-                 const std::vector<PassEval> &evals, unsigned long long *d_status) {
+                 const std::vector<PassEval> &evals, unsigned long long *d_status, int cov) {
   *pl = BFPlan();
+  pl->cov = cov;
   pl->precision = precision;
   pl->mode = mode;
   pl->nv = mode == 1 ? nv : 0;
@@ -191,6 +204,10 @@ int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   return NNGP_OK;
 }
 
+int nngp_bf_launch(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
+  return launch_pass(ctx, pl, fp32r, fallback_pass);
+}
+
 void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *pl) {
   for (void *p : pl->owned) nngp_free_async(ctx, p);
   pl->owned.clear();
@@ -225,4 +242,28 @@ int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches) {
   if (ms) *ms = total;
   return NNGP_OK;
 }
+}
+
+namespace {
+__global__ void prepare_coords_kernel(const double *__restrict__ cm, int n, double *__restrict__ xy,
+                                      float *__restrict__ xyf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = cm[i], y = cm[n + i];
+  if (xy) {
+    xy[2 * i] = x;
+    xy[2 * i + 1] = y;
+  }
+  if (xyf) {
+    const float hx = (float)x, hy = (float)y;
+    reinterpret_cast<float4 *>(xyf)[i] = make_float4(hx, hy, (float)(x - (double)hx), (float)(y - (double)hy));
+  }
+}
+}  // namespace
+
+int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf) {
+  if (n <= 0) return NNGP_OK;
+  prepare_coords_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(cm, n, xy, xyf);
+  NNGP_LAUNCH_CHECK(ctx);
+  return NNGP_OK;
 }

@@ -61,32 +61,49 @@ __device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) 
   return lo;
 }
 
-// Block-level fixed-order reduction of the per-thread values produced by `val(k)`
-// for k < ng; thread 0.. write out[k].
-template <int TPB, typename F>
-__device__ __forceinline__ void block_reduce_store(int ng, F val, double *wbuf, double *out) {
-  constexpr int W = TPB / 32;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = 0; k < ng; k++) {
-    const double s = warp_sum(val(k));
-    if (lane == 0) wbuf[w * kNGMax + k] = s;
-  }
-  __syncthreads();
-  for (int k = threadIdx.x; k < ng; k += TPB) {
-    double s = 0.0;
-#pragma unroll
-    for (int t = 0; t < W; t++) s += wbuf[t * kNGMax + k];
-    out[k] = s;
-  }
-}
-
 template <int M>
 __host__ __device__ constexpr int tri_size() { return M * (M + 1) / 2; }
 __host__ __device__ constexpr int tri_at(int r, int c) { return r * (r + 1) / 2 + c; }
 
+// Error-free transformations on the FP32 pipe (Knuth's TwoSum; TwoProduct by FMA),
+// as used by Ogita, Rump & Oishi's compensated dot product (Dot2, SIAM J. Sci.
+// Comput. 26, 2005): the refinement residual is accumulated as a float pair that
+// carries about twice float precision.  The _rn intrinsics keep the compiler from
+// contracting or reassociating them.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bv = __fsub_rn(s, a);
+  const float av = __fsub_rn(s, bv);
+  e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+// (s, e) with s + e = a - b exactly.
+__device__ __forceinline__ void two_diff(float a, float b, float &s, float &e) {
+  s = __fsub_rn(a, b);
+  const float bv = __fsub_rn(s, a);
+  const float av = __fsub_rn(s, bv);
+  e = __fsub_rn(__fsub_rn(a, av), __fadd_rn(b, bv));
+}
+// acc_hi + acc_lo += x * y with the product's rounding error carried.
+__device__ __forceinline__ void dot2_acc(float &hi, float &lo, float x, float y) {
+  const float p = __fmul_rn(x, y);
+  const float pe = __fmaf_rn(x, y, -p);
+  float q;
+  two_sum(hi, p, hi, q);
+  lo = __fadd_rn(lo, __fadd_rn(q, pe));
+}
+
+// v[k] for a runtime k < NNGP_MAX_NV without indexing a local array
+__device__ __forceinline__ double pick_nv(const double (&v)[NNGP_MAX_NV], int k) {
+  double r = 0.0;
+#pragma unroll
+  for (int t = 0; t < NNGP_MAX_NV; t++)
+    if (t == k) r = v[t];
+  return r;
+}
+
 // --------------------------------------------------------------------- kernel
-template <int M, bool R32, int MODE, int TPB>
-__global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ datas,
+template <int M, bool R32, int MODE, int TPB, int COV>
+__global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ datas,
                                                  const CovParams *__restrict__ thetas,
                                                  const BFJob *__restrict__ jobs, int njobs,
                                                  int total_tiles, int nv,
@@ -102,6 +119,7 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
   constexpr int GEO = R32 ? 4 : 2;
   double *wbuf = reinterpret_cast<double *>(geo + (size_t)GEO * M * TPB);
   const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
 #define TRI_(r, c) tri[(size_t)tri_at((r), (c)) * TPB + tid]
 #define GEO_(k, q) geo[(size_t)((k) * GEO + (q)) * TPB + tid]
 
@@ -115,31 +133,45 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
     const int i = tj * TPB + tid;
     bool active = i < d.n;
     if (active && only_flagged) active = job.flags[i] != 0;
+    // the flagged-only pass skips tiles with nothing to re-solve (block-uniform), leaving
+    // zero partial sums for them
+    if (only_flagged && !__syncthreads_or(active)) {
+      const int ngz = MODE == 0 ? 1 : 1 + nv * (nv + 1) / 2;
+      for (int k = tid; k < ngz; k += TPB) job.partial[(size_t)tj * ngz + k] = 0.0;
+      continue;
+    }
 
     int mi = 0, off = 0;
-    double xi = 0.0, yi = 0.0;
     int nb[M];
     if (active) {
       off = d.nnLU[i];
       mi = d.nnLU[d.n + i];
-      const double2 p = reinterpret_cast<const double2 *>(d.xy)[i];
-      xi = p.x;
-      yi = p.y;
     }
+    if constexpr (R32) {
+      // coordinates arrive split as float (hi, lo) pairs; differences stay exact to ~2^-48
+      const float4 pi4 = active ? reinterpret_cast<const float4 *>(d.xyf)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int k = 0; k < M; k++) {
-      nb[k] = 0;
-      if (k < mi) {
-        nb[k] = d.nnIndx[off + k];
-        const double2 q = reinterpret_cast<const double2 *>(d.xy)[nb[k]];
-        if constexpr (R32) {
-          const double ddx = q.x - xi, ddy = q.y - yi;
-          const float hx = (float)ddx, hy = (float)ddy;
+      for (int k = 0; k < M; k++) {
+        nb[k] = 0;
+        if (k < mi) {
+          nb[k] = d.nnIndx[off + k];
+          const float4 q = reinterpret_cast<const float4 *>(d.xyf)[nb[k]];
+          float hx, lx, hy, ly;
+          two_diff(q.x, pi4.x, hx, lx);
+          two_diff(q.y, pi4.y, hy, ly);
           GEO_(k, 0) = hx;
           GEO_(k, 1) = hy;
-          GEO_(k, 2) = (float)(ddx - (double)hx);
-          GEO_(k, 3) = (float)(ddy - (double)hy);
-        } else {
+          GEO_(k, 2) = __fadd_rn(lx, __fsub_rn(q.z, pi4.z));
+          GEO_(k, 3) = __fadd_rn(ly, __fsub_rn(q.w, pi4.w));
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        nb[k] = 0;
+        if (k < mi) {
+          nb[k] = d.nnIndx[off + k];
+          const double2 q = reinterpret_cast<const double2 *>(d.xy)[nb[k]];
           GEO_(k, 0) = q.x;
           GEO_(k, 1) = q.y;
         }
@@ -150,13 +182,21 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
     T cv[M];
     const T s2 = (T)sigmaSq, t2 = (T)tauSq;
     const float phif = (float)cpp->phi;
+    double xi = 0.0, yi = 0.0;
+    if constexpr (!R32) {
+      if (active) {
+        const double2 p = reinterpret_cast<const double2 *>(d.xy)[i];
+        xi = p.x;
+        yi = p.y;
+      }
+    }
 #pragma unroll
     for (int r = 0; r < M; r++) {
       cv[r] = (T)0;
       if (r < mi) {
         if constexpr (R32) {
           const float hx = GEO_(r, 0), hy = GEO_(r, 1);
-          cv[r] = s2 * nngp_cor_f(hx * hx + hy * hy, *cpp, phif);
+          cv[r] = s2 * nngp_cor_f<COV>(hx * hx + hy * hy, *cpp, phif);
 #pragma unroll
           for (int c = 0; c <= r; c++) {
             float e;
@@ -165,18 +205,18 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
             } else {
               const float ex = (GEO_(r, 0) - GEO_(c, 0)) + (GEO_(r, 2) - GEO_(c, 2));
               const float ey = (GEO_(r, 1) - GEO_(c, 1)) + (GEO_(r, 3) - GEO_(c, 3));
-              e = s2 * nngp_cor_f(ex * ex + ey * ey, *cpp, phif);
+              e = s2 * nngp_cor_f<COV>(ex * ex + ey * ey, *cpp, phif);
             }
             TRI_(r, c) = (T)e;
           }
         } else {
           const double xr = GEO_(r, 0), yr = GEO_(r, 1);
           const double ax = xi - xr, ay = yi - yr;
-          cv[r] = sigmaSq * nngp_cor_d(sqrt(ax * ax + ay * ay), *cpp);
+          cv[r] = sigmaSq * nngp_cor_d<COV>(sqrt(ax * ax + ay * ay), *cpp);
 #pragma unroll
           for (int c = 0; c <= r; c++) {
             const double bx = xr - GEO_(c, 0), by = yr - GEO_(c, 1);
-            double e = sigmaSq * nngp_cor_d(sqrt(bx * bx + by * by), *cpp);
+            double e = sigmaSq * nngp_cor_d<COV>(sqrt(bx * bx + by * by), *cpp);
             if (c == r) e += tauSq;
             TRI_(r, c) = (T)e;
           }
@@ -184,7 +224,8 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
       }
     }
 
-    // ---- Cholesky (row-oriented) fused with the forward solve L z = c
+    // ---- Cholesky (row-oriented) fused with the forward solve L z = c; two partial sums per
+    // inner product shorten the dependency chains
     T invd[M], z[M];
     bool ok = true;
 #pragma unroll
@@ -195,9 +236,14 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
         T row[M];
 #pragma unroll
         for (int c = 0; c <= r; c++) {
-          T s = TRI_(r, c);
+          T s0 = TRI_(r, c), s1 = (T)0;
 #pragma unroll
-          for (int k = 0; k < c; k++) s -= row[k] * ((c == r) ? row[k] : TRI_(c, k));
+          for (int k = 0; k < c; k++) {
+            const T l = (c == r) ? row[k] : TRI_(c, k);
+            if (k & 1) s1 -= row[k] * l;
+            else s0 -= row[k] * l;
+          }
+          const T s = s0 + s1;
           if (c < r) {
             row[c] = s * invd[c];
           } else {
@@ -207,10 +253,13 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
             invd[r] = (T)1 / dg;
           }
         }
-        T zs = cv[r];
+        T zs0 = cv[r], zs1 = (T)0;
 #pragma unroll
-        for (int k = 0; k < r; k++) zs -= row[k] * z[k];
-        z[r] = zs * invd[r];
+        for (int k = 0; k < r; k++) {
+          if (k & 1) zs1 -= row[k] * z[k];
+          else zs0 -= row[k] * z[k];
+        }
+        z[r] = (zs0 + zs1) * invd[r];
 #pragma unroll
         for (int c = 0; c <= r; c++) TRI_(r, c) = row[c];
       }
@@ -236,10 +285,13 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
         active = false;
         mi = 0;
       }
-      // ---- refinement: res = c - C b in FP64 with C rebuilt bit-identically
-      double res[M];
+      // ---- refinement residual res = c - C b, accumulated as a float pair (Dot2) with C rebuilt
+      float sh[M], sl[M];
 #pragma unroll
-      for (int r = 0; r < M; r++) res[r] = (r < mi) ? (double)cv[r] : 0.0;
+      for (int r = 0; r < M; r++) {
+        sh[r] = 0.f;
+        sl[r] = 0.f;
+      }
 #pragma unroll
       for (int r = 0; r < M; r++) {
         if (r < mi) {
@@ -251,11 +303,10 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
             } else {
               const float ex = (GEO_(r, 0) - GEO_(c, 0)) + (GEO_(r, 2) - GEO_(c, 2));
               const float ey = (GEO_(r, 1) - GEO_(c, 1)) + (GEO_(r, 3) - GEO_(c, 3));
-              e = s2 * nngp_cor_f(ex * ex + ey * ey, *cpp, phif);
+              e = s2 * nngp_cor_f<COV>(ex * ex + ey * ey, *cpp, phif);
             }
-            const double ed = (double)e;
-            res[r] = fma(-ed, (double)bb[c], res[r]);
-            if (c < r) res[c] = fma(-ed, (double)bb[r], res[c]);
+            dot2_acc(sh[r], sl[r], e, bb[c]);
+            if (c < r) dot2_acc(sh[c], sl[c], e, bb[r]);
           }
         }
       }
@@ -265,7 +316,7 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
       for (int r = 0; r < M; r++) {
         w[r] = (T)0;
         if (r < mi) {
-          T s = (T)res[r];
+          T s = __fsub_rn(__fsub_rn(cv[r], sh[r]), sl[r]);
 #pragma unroll
           for (int k = 0; k < r; k++) s -= TRI_(r, k) * w[k];
           w[r] = s * invd[r];
@@ -288,7 +339,7 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
     }
 
     // ---- F = sigma^2 + tau^2 - B'c in FP64
-    double Fi = sigmaSq + tauSq;
+    double Fi;
     {
       double dot = 0.0;
 #pragma unroll
@@ -314,7 +365,15 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
           if (k < mi) d.B[off + k] = Bd[k];
         d.F[i] = Fi;
       }
-      block_reduce_store<TPB>(1, [&](int) { return logF; }, wbuf, job.partial + (size_t)tj * 1);
+      const double s = warp_sum(logF);
+      if (lane == 0) wbuf[warp * kNGMax] = s;
+      __syncthreads();
+      if (tid == 0) {
+        double acc = 0.0;
+#pragma unroll
+        for (int t = 0; t < TPB / 32; t++) acc += wbuf[t * kNGMax];
+        job.partial[tj] = acc;
+      }
     } else {
       // r_v = V_i,v - sum_k B_k V_N(k),v for the nv columns, then r_a r_b / F
       double rv[NNGP_MAX_NV];
@@ -331,23 +390,28 @@ __global__ void __launch_bounds__(TPB) bf_kernel(const BFData *__restrict__ data
       }
       const double invF = active ? 1.0 / Fi : 0.0;
       const int ng = 1 + nv * (nv + 1) / 2;
-      block_reduce_store<TPB>(
-          ng,
-          [&](int k) -> double {
-            if (k == 0) return logF;
-            // k-1 enumerates (a, b), a <= b, row-major
-            int t = k - 1, a = 0;
-            while (t >= nv - a) { t -= nv - a; a++; }
-            const int b = a + t;
-            double ra = 0.0, rb = 0.0;
+      for (int k = 0; k < ng; k++) {
+        double val;
+        if (k == 0) {
+          val = logF;
+        } else {
+          int t = k - 1, a = 0;
+          while (t >= nv - a) {
+            t -= nv - a;
+            a++;
+          }
+          val = pick_nv(rv, a) * pick_nv(rv, a + t) * invF;
+        }
+        val = warp_sum(val);
+        if (lane == 0) wbuf[warp * kNGMax + k] = val;
+      }
+      __syncthreads();
+      for (int k = tid; k < ng; k += TPB) {
+        double acc = 0.0;
 #pragma unroll
-            for (int v = 0; v < NNGP_MAX_NV; v++) {
-              if (v == a) ra = rv[v];
-              if (v == b) rb = rv[v];
-            }
-            return ra * rb * invF;
-          },
-          wbuf, job.partial + (size_t)tj * ng);
+        for (int t = 0; t < TPB / 32; t++) acc += wbuf[t * kNGMax + k];
+        job.partial[(size_t)tj * ng + k] = acc;
+      }
     }
     __syncthreads();
   }
@@ -360,14 +424,14 @@ constexpr int bf_tpb() {
   return R32 ? (M <= 16 ? 128 : 64) : (M <= 16 ? 64 : 32);
 }
 
-template <int M, bool R32, int MODE>
+template <int M, bool R32, int MODE, int COV>
 int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass) {
   constexpr int TPB = bf_tpb<M, R32>();
   using T = typename std::conditional<R32, float, double>::type;
   constexpr int GEO = R32 ? 4 : 2;
   const size_t smem = sizeof(T) * ((size_t)tri_size<M>() + (size_t)GEO * M) * TPB +
                       sizeof(double) * (TPB / 32) * kNGMax;
-  auto kern = bf_kernel<M, R32, MODE, TPB>;
+  auto kern = bf_kernel<M, R32, MODE, TPB, COV>;
   static bool configured = false;  // once per instantiation
   if (!configured) {
     NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

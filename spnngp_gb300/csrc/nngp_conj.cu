@@ -105,6 +105,78 @@ __global__ void replicate_kernel(int ns, int n, int p, const double *__restrict_
   }
 }
 
+// Batched form of conj_fit_kernel: evaluation e belongs to a dataset of size ns[e].
+__global__ void conj_fit_multi_kernel(const double *__restrict__ out, int ng, int E, int p, const int *__restrict__ ns,
+                                      double aIG, double bIG, double *__restrict__ betaHat, double *__restrict__ ab,
+                                      double *__restrict__ bBInv, double *__restrict__ bb,
+                                      unsigned long long *__restrict__ status) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= E) return;
+  const int nv = p + 1;
+  const double *o = out + (size_t)k * ng;
+  double G[NNGP_MAX_NV * NNGP_MAX_NV];
+  int t = 1;
+  for (int a = 0; a < nv; a++)
+    for (int b = a; b < nv; b++) {
+      G[b * nv + a] = o[t];
+      G[a * nv + b] = o[t];
+      t++;
+    }
+  double V[(NNGP_MAX_NV - 1) * (NNGP_MAX_NV - 1)], v[NNGP_MAX_NV - 1], bh[NNGP_MAX_NV - 1];
+  for (int i = 0; i < p; i++) {
+    v[i] = G[p * nv + i];
+    for (int j = 0; j < p; j++) V[j * p + i] = (j <= i) ? G[j * nv + i] : 0.0;
+  }
+  if (!small_potrf(V, p)) {
+    atomicMin(status, (2ull << 48) | (unsigned long long)k);
+    return;
+  }
+  small_potri(V, p);
+  small_symv(V, p, v, bh);
+  double bv = 0.0;
+  for (int i = 0; i < p; i++) bv += bh[i] * v[i];
+  ab[2 * k] = aIG + 1.0 * ns[k] / 2.0;
+  ab[2 * k + 1] = bIG + 0.5 * (G[p * nv + p] - bv);
+  for (int i = 0; i < p; i++) {
+    betaHat[(size_t)k * p + i] = bh[i];
+    bb[(size_t)k * p + i] = v[i];
+  }
+  for (int i = 0; i < p * p; i++) bBInv[(size_t)k * p * p + i] = V[i];
+}
+
+// CRPS and RMSPE of one parameter set's predictions (R/util.R:247-255); block j scores
+// column j of the n0 x g prediction matrices, summing in a fixed order.
+__global__ void conj_score_kernel(const double *__restrict__ yTrue, const double *__restrict__ yHat,
+                                  const double *__restrict__ yVar, int n0, double *__restrict__ crps,
+                                  double *__restrict__ rmspe) {
+  const int j = blockIdx.x;
+  __shared__ double s1[256], s2[256];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n0; i += 256) {
+    const double yh = yHat[(size_t)j * n0 + i];
+    const double sd = sqrt(yVar[(size_t)j * n0 + i]);
+    const double z = (yTrue[i] - yh) / sd;
+    const double pdf = 0.3989422804014327 * exp(-0.5 * z * z);
+    a += -sd * (0.5641895835477563 - 2.0 * pdf - z * (2.0 * normcdf(z) - 1.0));
+    const double e = yTrue[i] - yh;
+    b += e * e;
+  }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      s1[threadIdx.x] += s1[threadIdx.x + w];
+      s2[threadIdx.x] += s2[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    crps[j] = s1[0] / n0;
+    rmspe[j] = sqrt(s2[0] / n0);
+  }
+}
+
 inline unsigned nb(long cnt, int tpb) { return (unsigned)((cnt + tpb - 1) / tpb); }
 
 struct Tmp {
@@ -186,6 +258,7 @@ int nngp_cNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, co
   const double *dX = (const double *)T.up(X, sizeof(double) * (size_t)n * p);
   const double *dy = (const double *)T.up(y, sizeof(double) * n);
   double *xy = (double *)T.up(nullptr, sizeof(double) * 2 * n);
+  float *xyf = (float *)T.up(nullptr, sizeof(float) * 4 * n);
   double *V = (double *)T.up(nullptr, sizeof(double) * (size_t)n * nv);
   std::vector<CovParams> th(g);
   for (int k = 0; k < g; k++)
@@ -199,9 +272,9 @@ int nngp_cNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, co
   double *dbb = (double *)T.up(nullptr, sizeof(double) * (size_t)p * g);
   unsigned long long *dst = (unsigned long long *)T.up(nullptr, sizeof(unsigned long long));
   if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
-  interleave_kernel3<<<nb(n, 256), 256, 0, ctx->stream>>>(dcm, n, xy);
+  nngp_prepare_coords(ctx, dcm, n, xy, xyf);
   build_v_kernel3<<<nb((long)n * nv, 256), 256, 0, ctx->stream>>>(dX, dy, n, p, V);
-  ctx->launches += 2;
+  ctx->launches += 1;
   int st = nngp_reset_status(ctx, dst);
   if (st) return st;
   BFData d{};
@@ -209,13 +282,14 @@ int nngp_cNNGP(nngp_ctx *ctx, const double *y, const double *X, int p, int n, co
   d.m = m;
   d.nv = nv;
   d.xy = xy;
+  d.xyf = xyf;
   d.nnIndx = dnn;
   d.nnLU = dlu;
   d.V = V;
   std::vector<PassEval> ev(g);
   for (int k = 0; k < g; k++) ev[k] = PassEval{0, k};
   BFPlan plan;
-  st = nngp_bf_plan(ctx, &plan, precision, 1, nv, {d}, dth, ev, dst);
+  st = nngp_bf_plan(ctx, &plan, precision, 1, nv, {d}, dth, ev, dst, nngp_plan_cov(th.data(), g));
   if (!st) st = nngp_bf_run(ctx, &plan, out);
   if (!st) {
     conj_fit_kernel<<<nb(g, 64), 64, 0, ctx->stream>>>(out, ng, g, p, n, sigmaSqIG[0], sigmaSqIG[1], dbeta, dab,
@@ -327,6 +401,7 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
   const double *dz = (const double *)T.up(normals, sizeof(double) * (size_t)n * nSamples);
   double *dy = (double *)T.up(nullptr, sizeof(double) * (size_t)n * nSamples);
   double *xy = (double *)T.up(nullptr, sizeof(double) * 2 * n);
+  float *xyf = (float *)T.up(nullptr, sizeof(float) * 4 * n);
   std::vector<CovParams> th(nSamples);
   for (int s = 0; s < nSamples; s++) {
     const double *t = theta + (size_t)s * nTheta;
@@ -341,8 +416,7 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
   double *dF = (double *)T.up(nullptr, sizeof(double) * (size_t)n * chunk);
   double *out = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)chunk);
   if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
-  interleave_kernel3<<<nb(n, 256), 256, 0, ctx->stream>>>(dcm, n, xy);
-  ctx->launches++;
+  nngp_prepare_coords(ctx, dcm, n, xy, xyf);
   int st = nngp_reset_status(ctx, dst);
   for (int s0 = 0; !st && s0 < nSamples; s0 += chunk) {
     const int ns = std::min(chunk, nSamples - s0);
@@ -353,6 +427,7 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
       d.n = n;
       d.m = m;
       d.xy = xy;
+      d.xyf = xyf;
       d.nnIndx = dnn;
       d.nnLU = dlu;
       d.B = dB + (size_t)t * (nI > 0 ? nI : 1);
@@ -361,7 +436,7 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
       ev[t] = PassEval{t, s0 + t};
     }
     BFPlan plan;
-    st = nngp_bf_plan(ctx, &plan, precision, 0, 0, datas, dth, ev, dst);
+    st = nngp_bf_plan(ctx, &plan, precision, 0, 0, datas, dth, ev, dst, nngp_plan_cov(th.data(), nSamples));
     if (!st) st = nngp_bf_run(ctx, &plan, out);
     if (!st) {
       replicate_kernel<<<nb(ns, 32), 32, 0, ctx->stream>>>(ns, n, p, dB, nI > 0 ? nI : 1, dF, dnn, dlu, dz, dX,
@@ -377,4 +452,140 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
   return NNGP_OK;
 }
 
+int nngp_cNNGP_multi(nngp_ctx *ctx, int nprob, const nngp_conj_problem *probs, int p, int m,
+                     const double *sigmaSqIG, int covModel, int precision, int resident) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (nprob < 1) return NNGP_OK;
+  if (p < 1 || p > NNGP_MAX_NV - 1) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= p <= 7 required");
+  if (m < 1 || m > NNGP_MAX_M) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= m <= 32 required");
+  if (covModel < 0 || covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+  for (int k = 0; k < nprob; k++)
+    if (probs[k].n < m || probs[k].g < 1 || probs[k].n0 < 0)
+      return nngp_fail(ctx, NNGP_ERR_ARG, "every problem needs n >= m, g >= 1 and n0 >= 0");
+  cudaSetDevice(ctx->device);
+  const int nTheta = covModel == 2 ? 3 : 2, nv = p + 1, ng = 1 + nv * (nv + 1) / 2;
+  Tmp T(ctx);
+  auto dev = [&](const void *h, size_t bytes) -> const void * { return resident ? h : T.up(h, bytes); };
+  std::vector<BFData> datas(nprob);
+  std::vector<CovParams> th;
+  std::vector<PassEval> ev;
+  std::vector<int> eoff(nprob), ns;
+  struct Dev {
+    const double *cm, *X, *y, *X0, *c0, *y0t;
+    const int *nn0;
+  };
+  std::vector<Dev> dv(nprob);
+  for (int k = 0; k < nprob; k++) {
+    const nngp_conj_problem &P = probs[k];
+    const int64_t nI = nngp_nindx(P.n, m);
+    Dev &D = dv[k];
+    D.cm = (const double *)dev(P.coords, sizeof(double) * 2 * P.n);
+    D.X = (const double *)dev(P.X, sizeof(double) * (size_t)P.n * p);
+    D.y = (const double *)dev(P.y, sizeof(double) * P.n);
+    const int *dnn = (const int *)dev(P.nnIndx, sizeof(int) * (nI > 0 ? nI : 0));
+    const int *dlu = (const int *)dev(P.nnIndxLU, sizeof(int) * 2 * P.n);
+    if (P.n0 > 0) {
+      D.X0 = (const double *)dev(P.X0, sizeof(double) * (size_t)P.n0 * p);
+      D.c0 = (const double *)dev(P.coords0, sizeof(double) * 2 * P.n0);
+      D.nn0 = (const int *)dev(P.nnIndx0, sizeof(int) * (size_t)P.n0 * m);
+      D.y0t = P.y0True ? (const double *)dev(P.y0True, sizeof(double) * P.n0) : nullptr;
+    }
+    double *xy = (double *)T.up(nullptr, sizeof(double) * 2 * P.n);
+    float *xyf = (float *)T.up(nullptr, sizeof(float) * 4 * P.n);
+    double *V = (double *)T.up(nullptr, sizeof(double) * (size_t)P.n * nv);
+    if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+    nngp_prepare_coords(ctx, D.cm, P.n, xy, xyf);
+    build_v_kernel3<<<nb((long)P.n * nv, 256), 256, 0, ctx->stream>>>(D.X, D.y, P.n, p, V);
+    ctx->launches++;
+    BFData d{};
+    d.n = P.n;
+    d.m = m;
+    d.nv = nv;
+    d.xy = xy;
+    d.xyf = xyf;
+    d.nnIndx = dnn;
+    d.nnLU = dlu;
+    d.V = V;
+    datas[k] = d;
+    eoff[k] = (int)th.size();
+    for (int j = 0; j < P.g; j++) {
+      const double *ta = P.thetaAlpha + (size_t)j * nTheta;
+      th.push_back(params(covModel, 1.0, ta[1], ta[0], covModel == 2 ? ta[2] : 0.0));
+      ev.push_back(PassEval{k, (int)th.size() - 1});
+      ns.push_back(P.n);
+    }
+  }
+  const int E = (int)th.size();
+  CovParams *dth = (CovParams *)T.up(th.data(), sizeof(CovParams) * E);
+  int *dns = (int *)T.up(ns.data(), sizeof(int) * E);
+  double *out = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)E * ng);
+  double *dbeta = (double *)T.up(nullptr, sizeof(double) * (size_t)p * E);
+  double *dab = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)E);
+  double *dV = (double *)T.up(nullptr, sizeof(double) * (size_t)p * p * E);
+  double *dbb = (double *)T.up(nullptr, sizeof(double) * (size_t)p * E);
+  unsigned long long *dst = (unsigned long long *)T.up(nullptr, sizeof(unsigned long long));
+  if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  int st = nngp_reset_status(ctx, dst);
+  if (st) return st;
+  BFPlan plan;
+  st = nngp_bf_plan(ctx, &plan, precision, 1, nv, datas, dth, ev, dst, nngp_plan_cov(th.data(), E));
+  if (!st) st = nngp_bf_run(ctx, &plan, out);
+  if (!st) {
+    conj_fit_multi_kernel<<<nb(E, 64), 64, 0, ctx->stream>>>(out, ng, E, p, dns, sigmaSqIG[0], sigmaSqIG[1], dbeta,
+                                                             dab, dV, dbb, dst);
+    ctx->launches++;
+  }
+  nngp_bf_plan_free(ctx, &plan);
+  if (st) return st;
+  if ((st = nngp_check_status(ctx, dst, "cNNGP"))) return st;
+  const cudaMemcpyKind back = resident ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  for (int k = 0; k < nprob; k++) {
+    const nngp_conj_problem &P = probs[k];
+    const int g = P.g, e0 = eoff[k];
+    if (P.n0 > 0 && (P.y0Hat || P.y0HatVar || (P.y0True && (P.crps || P.rmspe)))) {
+      PredArgs a{};
+      a.n = P.n;
+      a.m = m;
+      a.p = p;
+      a.n0 = P.n0;
+      a.npar = g;
+      a.xy = datas[k].xy;
+      a.V = datas[k].V;
+      a.c0 = dv[k].c0;
+      a.X0 = dv[k].X0;
+      a.nn0 = dv[k].nn0;
+      a.par = dth + e0;
+      a.beta = dbeta + (size_t)e0 * p;
+      a.Vinv = dV + (size_t)e0 * p * p;
+      a.ab = dab + 2 * (size_t)e0;
+      a.out0 = (double *)T.up(nullptr, sizeof(double) * (size_t)P.n0 * g);
+      a.out1 = (double *)T.up(nullptr, sizeof(double) * (size_t)P.n0 * g);
+      a.status = dst;
+      if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+      if ((st = run_pred(ctx, precision, KIND_CONJ, a, "cNNGP prediction"))) return st;
+      if (P.y0True && (P.crps || P.rmspe)) {
+        double *sc = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)g);
+        if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+        conj_score_kernel<<<g, 256, 0, ctx->stream>>>(dv[k].y0t, a.out0, a.out1, P.n0, sc, sc + g);
+        ctx->launches++;
+        if (P.crps) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.crps, sc, sizeof(double) * g, back, ctx->stream));
+        if (P.rmspe) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.rmspe, sc + g, sizeof(double) * g, back, ctx->stream));
+      }
+      if (P.y0Hat)
+        NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.y0Hat, a.out0, sizeof(double) * (size_t)P.n0 * g, back, ctx->stream));
+      if (P.y0HatVar)
+        NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.y0HatVar, a.out1, sizeof(double) * (size_t)P.n0 * g, back, ctx->stream));
+    }
+    if (P.betaHat)
+      NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.betaHat, dbeta + (size_t)e0 * p, sizeof(double) * p * g, back, ctx->stream));
+    if (P.ab) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.ab, dab + 2 * (size_t)e0, sizeof(double) * 2 * g, back, ctx->stream));
+    if (P.bBInv)
+      NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.bBInv, dV + (size_t)e0 * p * p, sizeof(double) * p * p * g, back, ctx->stream));
+    if (P.bb) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(P.bb, dbb + (size_t)e0 * p, sizeof(double) * p * g, back, ctx->stream));
+  }
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return NNGP_OK;
+}
+
 }  // extern "C"
+

@@ -25,7 +25,7 @@ enum ScratchSlot {
   S_COORDS = 0, S_NNINDX, S_NNLU, S_B, S_F, S_V, S_PARTIAL, S_RED, S_THETA, S_STATUS,
   S_U, S_V2, S_IDX, S_IDX2, S_SORT_TMP, S_XS, S_YS, S_OS, S_NNDIST, S_COORDS0,
   S_NNINDX0, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4, S_OUT5, S_STREAM_N, S_STREAM_U,
-  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_NUM_SLOTS
+  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_XYF, S_NUM_SLOTS
 };
 
 struct BFPlan;
@@ -127,6 +127,7 @@ __host__ __device__ inline void cov_prepare(CovParams &c) {
 struct BFData {
   int n, m, nv;
   const double *xy;      // n x 2 interleaved (x, y)
+  const float *xyf;      // n x 4 (x hi, y hi, x lo, y lo): the FP32R kernels' coordinates
   const int *nnIndx;     // packed neighbor lists
   const int *nnLU;       // [offsets | counts], 2n
   const double *V;       // n x nv row-major, fused pass only
@@ -149,6 +150,7 @@ struct BFJob {
 // run time, so callers may rewrite them between runs.
 struct BFPlan {
   int precision = 0, mode = 0, mmax = 0, nv = 0, ng = 0;
+  int cov = 4;  // NNGP_COV_* code of the kernels the plan runs (NNGP_COV_ANY: any parameter set)
   int njobs = 0, tiles = 0, tiles_fb = 0;
   BFData *d_datas = nullptr;
   const CovParams *d_thetas = nullptr;
@@ -163,10 +165,29 @@ struct PassEval {
   int data;
   int theta;
 };
-// Builds a plan (device allocations owned by the plan, stream-ordered).
+// Correlation-function codes the B/F kernels are compiled for: a kernel compiled for one
+// model evaluates only that formula; NNGP_COV_ANY switches on each parameter set's model and
+// is the only one that carries the general-nu Matern evaluation.
+enum : int { NNGP_COV_EXP = 0, NNGP_COV_SPH = 1, NNGP_COV_MAT_HALF = 2, NNGP_COV_GAU = 3, NNGP_COV_ANY = 4 };
+// Builds a plan (device allocations owned by the plan, stream-ordered).  cov must cover every
+// parameter set the plan will ever run with (see nngp_plan_cov).
 int nngp_bf_plan(nngp_ctx *ctx, BFPlan *plan, int precision, int mode, int nv,
                  const std::vector<BFData> &datas, const CovParams *d_thetas,
-                 const std::vector<PassEval> &evals, unsigned long long *d_status);
+                 const std::vector<PassEval> &evals, unsigned long long *d_status, int cov = NNGP_COV_ANY);
+// The narrowest kernel code covering these (fixed) parameter sets: their common model, with
+// Matern only when every nu is k + 1/2 (k <= 8); NNGP_COV_ANY otherwise.
+inline int nngp_plan_cov(const CovParams *cps, int count) {
+  if (count < 1) return NNGP_COV_ANY;
+  const int model = cps[0].model;
+  for (int k = 0; k < count; k++) {
+    if (cps[k].model != model) return NNGP_COV_ANY;
+    if (model == 2 && cps[k].halfk < 0) return NNGP_COV_ANY;
+  }
+  return model;
+}
+// Launches the kernel instantiation the plan needs (primary pass, or the FP64 re-solve of the
+// flagged locations when fallback_pass).
+int nngp_bf_launch(nngp_ctx *ctx, const BFPlan *plan, bool fp32r, bool fallback_pass);
 // Launches the pass; d_out receives njobs x ng sums (log F first, then the Gram
 // entries r_a r_b / F over a <= b, row-major).
 int nngp_bf_run(nngp_ctx *ctx, const BFPlan *plan, double *d_out);
@@ -174,6 +195,10 @@ void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *plan);
 // Stream-ordered device allocation (pooled), freed with nngp_free_async.
 void *nngp_malloc_async(nngp_ctx *ctx, size_t bytes);
 void nngp_free_async(nngp_ctx *ctx, void *p);
+
+// Writes the interleaved double coordinates (xy, may be null) and their float hi/lo
+// split (xyf, may be null) from the n x 2 column-major coordinates.
+int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf);
 
 // Device status word: 0xFFFF..FF = ok, otherwise (code << 48) | location.
 constexpr unsigned long long NNGP_STATUS_OK = ~0ull;

@@ -25,30 +25,26 @@
 // locations listing it in increasing order, and the entry positions give uiIndx.
 #include <cuda_runtime.h>
 #include <cub/cub.cuh>
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 #include "nngp_internal.h"
 
 namespace {
 
-__device__ __forceinline__ bool gt_nan_last(double a, double b) {
-  const bool na = isnan(a), nb = isnan(b);
-  if (na && nb) return false;
-  if (na) return true;
-  if (nb) return false;
-  return a > b;
-}
-
-// R's rsort_with_index: Shell sort, Knuth gaps starting above n/9, NaN last.
-__device__ void shell_sort_idx(double *x, int *idx, int n) {
+// The neighbor lists hold non-negative distances (or +inf), whose IEEE bit patterns
+// order exactly like signed 64-bit integers, so the lists keep the bit patterns and
+// compare them on the integer pipe.  R's Shell sort on such keys:
+__device__ void shell_sort_keys(long long *x, int *idx, int n) {
   int gap = 1;
   while (gap <= n / 9) gap = 3 * gap + 1;
   for (; gap > 0; gap /= 3) {
     for (int i = gap; i < n; i++) {
-      const double key = x[i];
+      const long long key = x[i];
       const int tag = idx[i];
       int j = i;
-      while (j >= gap && gt_nan_last(x[j - gap], key)) {
+      while (j >= gap && x[j - gap] > key) {
         x[j] = x[j - gap];
         idx[j] = idx[j - gap];
         j -= gap;
@@ -57,6 +53,36 @@ __device__ void shell_sort_idx(double *x, int *idx, int n) {
       idx[j] = tag;
     }
   }
+}
+
+// Replaces the last (worst) entry of a sorted list by (key, tag) and re-sorts it exactly as
+// R's rsort_with_index would.  While the list holds no equal keys and the new key equals none
+// of them, every sort yields the same order, so a plain insertion is used; once a tie exists
+// the Shell sort itself runs (it may reorder tied entries).
+__device__ __forceinline__ void list_insert(long long *x, int *idx, int n, long long key, int tag, bool &ties) {
+  if (!ties) {
+    int j = n - 1;
+    while (j > 0 && x[j - 1] > key) {
+      x[j] = x[j - 1];
+      idx[j] = idx[j - 1];
+      j--;
+    }
+    if (j > 0 && x[j - 1] == key) {
+      // undo the shifts and hand the list to the exact sort
+      for (int t = j; t < n - 1; t++) {
+        x[t] = x[t + 1];
+        idx[t] = idx[t + 1];
+      }
+      ties = true;
+    } else {
+      x[j] = key;
+      idx[j] = tag;
+      return;
+    }
+  }
+  x[n - 1] = key;
+  idx[n - 1] = tag;
+  shell_sort_keys(x, idx, n);
 }
 
 // Packed-list offset / length of location i (src/util.cpp:55-70).
@@ -89,6 +115,15 @@ __global__ void tie_kernel(const double *__restrict__ us, int n, int *__restrict
   }
 }
 
+// R's comparison for rsort_with_index on arbitrary doubles: NaN sorts last.
+__device__ __forceinline__ bool gt_nan_last(double a, double b) {
+  const bool na = isnan(a), nb = isnan(b);
+  if (na && nb) return false;
+  if (na) return true;
+  if (nb) return false;
+  return a > b;
+}
+
 // One gap pass of the Shell sort: thread c owns the chain c, c+h, c+2h, ...
 __global__ void shell_pass_kernel(double *__restrict__ u, int *__restrict__ idx, int n, int h) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,88 +143,146 @@ __global__ void shell_pass_kernel(double *__restrict__ u, int *__restrict__ idx,
 }
 
 __global__ void gather_sorted_kernel(const double *__restrict__ cm, int n, const int *__restrict__ sidx,
-                                     double *__restrict__ xs, double *__restrict__ ys) {
+                                     double *__restrict__ xs, double *__restrict__ ys, float4 *__restrict__ sf,
+                                     double cx, double cy) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n) {
     const int j = sidx[s];
-    xs[s] = cm[j];
-    ys[s] = cm[n + j];
+    const double x = cm[j], y = cm[n + j];
+    xs[s] = x;
+    ys[s] = y;
+    if (sf) sf[s] = make_float4((float)(x - cx), (float)(y - cy), __int_as_float(j), 0.f);
   }
 }
 
-// Code-book search for the location at sorted position s.
+// Extent of the coordinates: out = (min x, max x, min y, max y) as ordered-integer keys.
+__device__ __forceinline__ unsigned long long dkey(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dval(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+__global__ void extent_kernel(const double *__restrict__ cm, int n, unsigned long long *__restrict__ out) {
+  unsigned long long mnx = ~0ull, mxx = 0, mny = ~0ull, mxy = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long kx = dkey(cm[i]), ky = dkey(cm[n + i]);
+    mnx = min(mnx, kx);
+    mxx = max(mxx, kx);
+    mny = min(mny, ky);
+    mxy = max(mxy, ky);
+  }
+  atomicMin(&out[0], mnx);
+  atomicMax(&out[1], mxx);
+  atomicMin(&out[2], mny);
+  atomicMax(&out[3], mxy);
+}
+
+// Error bounds of the float pre-filter (unit roundoff u = 2^-24, FP64 e = 2^-53):
+// coordinates are stored as x' = fl32(fl64(x - cx)); with S the largest |x - cx|, |y - cy|
+// and M the largest |x|, |y|:
+//   |fl32(x'_j - x'_q) - (x_j - x_q)| <= 5 u S                          (Ex)
+//   |fl32(fx + fy) - du_ref|            <= 15 u S + 12 e M               (Eu)
+// where du_ref is the reference's FP64 ((x_q + y_q) - x_j) - y_j up to sign.
+struct FilterConsts {
+  float ex, eu;
+};
+
+// Thresholds derived from the current worst squared distance W (rare: only on inserts).
+struct FilterThr {
+  float p0, p1, ins;  // |fu| <= p0: surely not pruned; |fu| > p1: surely pruned; lb >= ins: surely not inserted
+};
+__device__ __forceinline__ FilterThr make_thr(double W, const FilterConsts &fc) {
+  FilterThr t;
+  const double e64 = 1.1102230246251565e-16;
+  const float hi = __double2float_ru(2.0 * W * (1.0 + 4 * e64));
+  const float lo = __double2float_rd(2.0 * W * (1.0 - 4 * e64));
+  t.p1 = __fadd_ru(__fsqrt_ru(hi), fc.eu);
+  t.p0 = __fsub_rd(__fsqrt_rd(lo), fc.eu);
+  t.ins = __double2float_ru(W * (1.0 + 8 * e64));
+  return t;
+}
+// Lower bound (rounded down) of the candidate's true squared distance.
+__device__ __forceinline__ float lower_de(float fx, float fy, const FilterConsts &fc) {
+  const float ax = fmaxf(__fsub_rd(fabsf(fx), fc.ex), 0.f);
+  const float ay = fmaxf(__fsub_rd(fabsf(fy), fc.ex), 0.f);
+  return __fadd_rd(__fmul_rd(ax, ax), __fmul_rd(ay, ay));
+}
+
+// Code-book search for the location at sorted position s.  Each candidate is first
+// classified in float with rigorous error bounds (surely pruned / surely kept / surely
+// not inserted); only candidates the bounds cannot decide are evaluated with the
+// reference's exact FP64 arithmetic, so every decision equals the reference's.
 __global__ void __launch_bounds__(128) cb_kernel(int n, int m, const double *__restrict__ xs,
-                                                 const double *__restrict__ ys, const int *__restrict__ os,
-                                                 int *__restrict__ nnIndx, double *__restrict__ nnDist,
-                                                 int *__restrict__ nnLU) {
+                                                 const double *__restrict__ ys, const float4 *__restrict__ sf,
+                                                 FilterConsts fc, int *__restrict__ nnIndx,
+                                                 double *__restrict__ nnDist, int *__restrict__ nnLU) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const int q = os[s];
+  const float4 me = sf[s];
+  const int q = __float_as_int(me.z);
   int off, cnt;
   nn_slot(q, m, off, cnt);
   nnLU[q] = off;
   nnLU[n + q] = cnt;
   if (cnt == 0) return;
-  double dl[NNGP_MAX_M_SEARCH];
+  long long kl[NNGP_MAX_M_SEARCH];
   int il[NNGP_MAX_M_SEARCH];
   for (int k = 0; k < cnt; k++) {
-    dl[k] = __longlong_as_double(0x7ff0000000000000ll);
+    kl[k] = 0x7ff0000000000000ll;  // +inf
     il[k] = 0;
   }
-  double worst = dl[0];
+  // the +inf fillers are identical (key, tag) pairs, so their mutual order never shows
+  bool ties = false;
+  double worst = __longlong_as_double(0x7ff0000000000000ll);
+  FilterThr thr = make_thr(worst, fc);
   const double qx = xs[s], qy = ys[s];
   const double qu = __dadd_rn(qx, qy);
   int lo = s, hi = s;
   bool down = true, up = true;
+  // one step of the walk at sorted position t; returns false when the direction stops
+  auto visit = [&](int t) -> bool {
+    const float4 c = sf[t];
+    const float fx = __fsub_rn(c.x, me.x), fy = __fsub_rn(c.y, me.y);
+    const float fu = fabsf(__fadd_rn(fx, fy));
+    if (fu > thr.p1) return false;  // (u_q - u_j)^2 > 2 worst for sure
+    if (!(fu <= thr.p0)) {          // undecided: the reference's own test
+      const double du = __dadd_rn(__dadd_rn(qu, -xs[t]), -ys[t]);
+      if (__dmul_rn(du, du) > 2.0 * worst) return false;
+    }
+    const int j = __float_as_int(c.z);
+    if (j < q && !(lower_de(fx, fy, fc) >= thr.ins)) {
+      const double dx = __dadd_rn(qx, -xs[t]), dy = __dadd_rn(qy, -ys[t]);
+      const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      if (de < worst) {
+        list_insert(kl, il, cnt, __double_as_longlong(de), j, ties);
+        worst = __longlong_as_double(kl[cnt - 1]);
+        if (ties) {
+          // the exact sort is needed only while equal finite keys remain in the list
+          bool any = false;
+          for (int t = 1; t < cnt; t++) any |= (kl[t] == kl[t - 1] && kl[t] != 0x7ff0000000000000ll);
+          ties = any;
+        }
+        thr = make_thr(worst, fc);
+      }
+    }
+    return true;
+  };
   while (down || up) {
     if (lo == 0) down = false;
     if (hi == n - 1) up = false;
     if (down) {
       lo--;
-      const double cx = xs[lo], cy = ys[lo];
-      const double du = __dadd_rn(__dadd_rn(qu, -cx), -cy);
-      const double dm = __dmul_rn(du, du);
-      if (dm > 2.0 * worst) {
-        down = false;
-      } else {
-        const int j = os[lo];
-        if (j < q) {
-          const double dx = __dadd_rn(qx, -cx), dy = __dadd_rn(qy, -cy);
-          const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-          if (de < worst) {
-            dl[cnt - 1] = de;
-            il[cnt - 1] = j;
-            shell_sort_idx(dl, il, cnt);
-            worst = dl[cnt - 1];
-          }
-        }
-      }
+      if (!visit(lo)) down = false;
     }
     if (up) {
       hi++;
-      const double cx = xs[hi], cy = ys[hi];
-      const double du = __dadd_rn(__dadd_rn(qu, -cx), -cy);
-      const double dm = __dmul_rn(du, du);
-      if (dm > 2.0 * worst) {
-        up = false;
-      } else {
-        const int j = os[hi];
-        if (j < q) {
-          const double dx = __dadd_rn(qx, -cx), dy = __dadd_rn(qy, -cy);
-          const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-          if (de < worst) {
-            dl[cnt - 1] = de;
-            il[cnt - 1] = j;
-            shell_sort_idx(dl, il, cnt);
-            worst = dl[cnt - 1];
-          }
-        }
-      }
+      if (!visit(hi)) up = false;
     }
   }
   for (int k = 0; k < cnt; k++) {
     nnIndx[off + k] = il[k];
-    nnDist[off + k] = __dsqrt_rn(dl[k]);
+    nnDist[off + k] = __dsqrt_rn(__longlong_as_double(kl[k]));
   }
 }
 
@@ -204,13 +297,14 @@ __global__ void __launch_bounds__(128) brute_kernel(int n, int m, const double *
   nnLU[i] = off;
   nnLU[n + i] = cnt;
   if (cnt == 0) return;
-  double dl[NNGP_MAX_M_SEARCH];
+  long long kl[NNGP_MAX_M_SEARCH];
   int il[NNGP_MAX_M_SEARCH];
   for (int k = 0; k < cnt; k++) {
-    dl[k] = __longlong_as_double(0x7ff0000000000000ll);
+    kl[k] = 0x7ff0000000000000ll;
     il[k] = 0;
   }
-  double worst = dl[0];
+  bool ties = false;
+  double worst = __longlong_as_double(0x7ff0000000000000ll);
   double thr = worst;  // squared distances above thr cannot beat worst
   const double xi = cm[i], yi = cm[n + i];
   for (int j = 0; j < i; j++) {
@@ -219,16 +313,19 @@ __global__ void __launch_bounds__(128) brute_kernel(int n, int m, const double *
     if (de > thr) continue;
     const double d = __dsqrt_rn(de);
     if (d < worst) {
-      dl[cnt - 1] = d;
-      il[cnt - 1] = j;
-      shell_sort_idx(dl, il, cnt);
-      worst = dl[cnt - 1];
+      list_insert(kl, il, cnt, __double_as_longlong(d), j, ties);
+      worst = __longlong_as_double(kl[cnt - 1]);
+      if (ties) {
+        bool any = false;
+        for (int t = 1; t < cnt; t++) any |= (kl[t] == kl[t - 1] && kl[t] != 0x7ff0000000000000ll);
+        ties = any;
+      }
       thr = worst * worst * (1.0 + 1e-12);
     }
   }
   for (int k = 0; k < cnt; k++) {
     nnIndx[off + k] = il[k];
-    nnDist[off + k] = dl[k];
+    nnDist[off + k] = __longlong_as_double(kl[k]);
   }
 }
 
@@ -341,7 +438,7 @@ inline unsigned blocks(long cnt, int tpb) { return (unsigned)((cnt + tpb - 1) / 
 
 // Sorts (u, index) and builds the sorted SoA view.  coords: device, column-major.
 int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **ys, int **os,
-                double **us, bool exact_ties) {
+                double **us, bool exact_ties, float4 **sf, FilterConsts &fc) {
   double *u, *u2;
   int *idx, *idx2;
   NNGP_ALLOC(ctx, u, double, S_U, (size_t)n);
@@ -379,9 +476,34 @@ int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **
       NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(idx2, idx, sizeof(int) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     }
   }
+  // extent of the coordinates for the float pre-filter's error bounds
+  unsigned long long *ext;
+  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
+  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(d_cm, n, ext);
+  NNGP_LAUNCH_CHECK(ctx);
+  unsigned long long hk[4];
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  auto hval = [](unsigned long long k) {
+    unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    double v;
+    memcpy(&v, &b, sizeof v);
+    return v;
+  };
+  const double mnx = hval(hk[0]), mxx = hval(hk[1]), mny = hval(hk[2]), mxy = hval(hk[3]);
+  const double cx = 0.5 * (mnx + mxx), cy = 0.5 * (mny + mxy);
+  const double S = std::max(std::max(mxx - cx, cx - mnx), std::max(mxy - cy, cy - mny)) * (1.0 + 1e-12);
+  const double M = std::max(std::max(std::fabs(mnx), std::fabs(mxx)), std::max(std::fabs(mny), std::fabs(mxy)));
+  const double u32 = 5.9604644775390625e-08, e64 = 1.1102230246251565e-16;
+  fc.ex = (float)((5 * u32 * S + 4 * e64 * M) * 1.001);
+  fc.eu = (float)((15 * u32 * S + 12 * e64 * M) * 1.001);
+  if (!std::isfinite(S) || !std::isfinite(M)) fc.ex = fc.eu = __builtin_inff();
   NNGP_ALLOC(ctx, *xs, double, S_XS, (size_t)n);
   NNGP_ALLOC(ctx, *ys, double, S_YS, (size_t)n);
-  gather_sorted_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(d_cm, n, idx2, *xs, *ys);
+  NNGP_ALLOC(ctx, *sf, float4, S_OS, (size_t)n);
+  gather_sorted_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(d_cm, n, idx2, *xs, *ys, *sf, cx, cy);
   NNGP_LAUNCH_CHECK(ctx);
   *os = idx2;
   if (us) *us = u2;
@@ -407,8 +529,10 @@ int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *
   cudaSetDevice(ctx->device);
   double *xs, *ys;
   int *os;
-  if ((st = sorted_view(ctx, n, coords, &xs, &ys, &os, nullptr, true))) return st;
-  cb_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, xs, ys, os, nnIndx, nnDist, nnIndxLU);
+  float4 *sf;
+  FilterConsts fc;
+  if ((st = sorted_view(ctx, n, coords, &xs, &ys, &os, nullptr, true, &sf, fc))) return st;
+  cb_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, xs, ys, sf, fc, nnIndx, nnDist, nnIndxLU);
   NNGP_LAUNCH_CHECK(ctx);
   NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return NNGP_OK;
@@ -461,6 +585,24 @@ int nngp_mkNNIndx(nngp_ctx *ctx, int n, int m, const double *coords, int *nnIndx
   return NNGP_OK;
 }
 
+int nngp_nn2_dev(nngp_ctx *ctx, int n, const double *coords, int n0, const double *coords0, int k,
+                 int *nnIdx, double *nnDist) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (n < 1 || n0 < 0 || k < 1 || k > NNGP_MAX_M_SEARCH || k > n)
+    return nngp_fail(ctx, NNGP_ERR_ARG, "nn2 needs 1 <= k <= min(n, 64)");
+  if (n0 == 0) return NNGP_OK;
+  cudaSetDevice(ctx->device);
+  double *xs, *ys, *us;
+  int *os;
+  float4 *sf;
+  FilterConsts fc;
+  int st = sorted_view(ctx, n, coords, &xs, &ys, &os, &us, false, &sf, fc);
+  if (st) return st;
+  nn2_kernel<<<blocks(n0, 128), 128, 0, ctx->stream>>>(n, xs, ys, os, us, n0, coords0, k, nnIdx, nnDist);
+  NNGP_LAUNCH_CHECK(ctx);
+  return NNGP_OK;
+}
+
 int nngp_nn2(nngp_ctx *ctx, int n, const double *coords, int n0, const double *coords0, int k,
              int *nnIdx, double *nnDist) {
   if (!ctx) return NNGP_ERR_ARG;
@@ -476,12 +618,8 @@ int nngp_nn2(nngp_ctx *ctx, int n, const double *coords, int n0, const double *c
   NNGP_ALLOC(ctx, dd, double, S_OUT0, (size_t)n0 * k);
   NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(cm, coords, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
   NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(c0, coords0, sizeof(double) * 2 * n0, cudaMemcpyHostToDevice, ctx->stream));
-  double *xs, *ys, *us;
-  int *os;
-  int st = sorted_view(ctx, n, cm, &xs, &ys, &os, &us, false);
+  int st = nngp_nn2_dev(ctx, n, cm, n0, c0, k, di, dd);
   if (st) return st;
-  nn2_kernel<<<blocks(n0, 128), 128, 0, ctx->stream>>>(n, xs, ys, os, us, n0, c0, k, di, dd);
-  NNGP_LAUNCH_CHECK(ctx);
   NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnIdx, di, sizeof(int) * n0 * k, cudaMemcpyDeviceToHost, ctx->stream));
   if (nnDist)
     NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(nnDist, dd, sizeof(double) * n0 * k, cudaMemcpyDeviceToHost, ctx->stream));

@@ -113,9 +113,24 @@ __device__ inline double nngp_matern_d(double x, const CovParams &cp) {
   return cp.mconst * pow(x, cp.nu) * nngp_bessel_k(x, cp.nu);
 }
 
+// COV (NNGP_COV_* of nngp_internal.h) selects the formula at compile time: a kernel compiled
+// for one model carries no switch and no dead branches in its unrolled covariance build.
+
+// Matern with nu = k + 1/2: exp(-x) * poly(x), x = phi d.
+template <typename R>
+__device__ inline R nngp_matern_half(R x, const CovParams &cp) {
+  R s = (R)cp.poly[cp.halfk];
+#pragma unroll 1
+  for (int j = cp.halfk - 1; j >= 0; j--) s = s * x + (R)cp.poly[j];
+  if constexpr (sizeof(R) == 4) return expf(-x) * s;
+  else return exp(-x) * s;
+}
+
 // Correlation (no sigma^2) at distance d, FP64.
+template <int COV = NNGP_COV_ANY>
 __device__ inline double nngp_cor_d(double d, const CovParams &cp) {
-  switch (cp.model) {
+  const int model = COV == NNGP_COV_ANY ? cp.model : COV;
+  switch (model) {
     case 0:
       return exp(-cp.phi * d);
     case 1: {
@@ -128,7 +143,9 @@ __device__ inline double nngp_cor_d(double d, const CovParams &cp) {
     }
     case 2: {
       const double x = d * cp.phi;
-      return (x > 0.0) ? nngp_matern_d(x, cp) : 1.0;
+      if (!(x > 0.0)) return 1.0;
+      if constexpr (COV == NNGP_COV_ANY) return nngp_matern_d(x, cp);
+      return nngp_matern_half(x, cp);
     }
     default: {
       const double t = cp.phi * d;
@@ -138,9 +155,11 @@ __device__ inline double nngp_cor_d(double d, const CovParams &cp) {
 }
 
 // Correlation in FP32 from a squared distance d2 (the refined path).  Matern at a
-// general nu goes through the FP64 Bessel evaluation.
+// general nu goes through the FP64 Bessel evaluation (NNGP_COV_ANY only).
+template <int COV = NNGP_COV_ANY>
 __device__ inline float nngp_cor_f(float d2, const CovParams &cp, float phif) {
-  switch (cp.model) {
+  const int model = COV == NNGP_COV_ANY ? cp.model : COV;
+  switch (model) {
     case 0:
       return expf(-phif * sqrtf(d2));
     case 1: {
@@ -152,12 +171,10 @@ __device__ inline float nngp_cor_f(float d2, const CovParams &cp, float phif) {
     case 2: {
       const float x = phif * sqrtf(d2);
       if (!(x > 0.0f)) return 1.0f;
-      if (cp.halfk >= 0) {
-        float s = (float)cp.poly[cp.halfk];
-        for (int j = cp.halfk - 1; j >= 0; j--) s = s * x + (float)cp.poly[j];
-        return expf(-x) * s;
+      if constexpr (COV == NNGP_COV_ANY) {
+        if (cp.halfk < 0) return (float)nngp_matern_d((double)x, cp);
       }
-      return (float)nngp_matern_d((double)x, cp);
+      return nngp_matern_half(x, cp);
     }
     default:
       return expf(-(phif * phif) * d2);

@@ -45,6 +45,7 @@ struct MCConst {
   const double *B;     // standalone pass outputs (replicates)
   const double *F;
   const int *nnIndx, *nnLU;
+  const double *out;   // this instance's (log F, Gram) sums in its size class's output buffer
 };
 
 struct MCState {
@@ -117,12 +118,11 @@ __device__ inline void unpack(const double *o, int nv, double &ld, double *G) {
     }
 }
 
-__global__ void mc_init_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts,
-                               const double *__restrict__ out, int ng, int ninst) {
+__global__ void mc_init_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts, int ninst) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ninst) return;
   MCState &st = sts[k];
-  unpack(out + (size_t)k * ng, cs[k].p + 1, st.ld, st.G);
+  unpack(cs[k].out, cs[k].p + 1, st.ld, st.G);
   st.thetaUpdate = 1;
 }
 
@@ -180,8 +180,7 @@ __global__ void mc_pre_kernel(const MCConst *__restrict__ cs, MCState *__restric
 }
 
 __global__ void mc_post_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts,
-                               CovParams *__restrict__ thetas, const double *__restrict__ out, int ng,
-                               int ninst) {
+                               CovParams *__restrict__ thetas, int ninst) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ninst) return;
   const MCConst &c = cs[k];
@@ -189,7 +188,7 @@ __global__ void mc_post_kernel(const MCConst *__restrict__ cs, MCState *__restri
   if (st.status || st.s >= c.nSamples) return;
   const int p = c.p, nv = p + 1;
   double ld, G[NNGP_MAX_NV * NNGP_MAX_NV];
-  unpack(out + (size_t)k * ng, nv, ld, G);
+  unpack(c.out, nv, ld, G);
   const double q = quad_from_gram(G, p, st.beta);
   const double lpCand = log_post(c, ld, q, st.cand);
   double u = 0.5;
@@ -232,17 +231,6 @@ __global__ void mc_rep_kernel(const MCConst *__restrict__ cs, MCState *__restric
     out[i] += xb;
   }
   st.repCnt++;
-}
-
-// Every block of the standalone pass checks whether this iteration draws a replicate.
-__global__ void noop_kernel() {}
-
-__global__ void interleave_kernel2(const double *__restrict__ cm, int n, double *__restrict__ xy) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    xy[2 * i] = cm[i];
-    xy[2 * i + 1] = cm[n + i];
-  }
 }
 
 __global__ void build_v_kernel(const double *__restrict__ X, const double *__restrict__ y, int n, int p,
@@ -302,19 +290,21 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     const MCInstance &I = insts[k];
     if (I.p != p) return nngp_fail(ctx, NNGP_ERR_ARG, "instances of one batch must share p");
     double *xy = (double *)own(sizeof(double) * 2 * I.n);
+    float *xyf = precision == NNGP_FP32R ? (float *)own(sizeof(float) * 4 * I.n) : nullptr;
     double *V = (double *)own(sizeof(double) * (size_t)I.n * nv);
-    if (!xy || !V) {
+    if (!xy || !V || (precision == NNGP_FP32R && !xyf)) {
       release();
       return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
     }
-    interleave_kernel2<<<nblk(I.n, 256), 256, 0, ctx->stream>>>(I.coords_cm, I.n, xy);
+    nngp_prepare_coords(ctx, I.coords_cm, I.n, xy, xyf);
     build_v_kernel<<<nblk((long)I.n * nv, 256), 256, 0, ctx->stream>>>(I.X, I.y, I.n, p, V);
-    ctx->launches += 2;
+    ctx->launches += 1;
     BFData d{};
     d.n = I.n;
     d.m = I.m;
     d.nv = nv;
     d.xy = xy;
+    d.xyf = xyf;
     d.nnIndx = I.nnIndx;
     d.nnLU = I.nnLU;
     d.V = V;
@@ -364,13 +354,40 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     cov_prepare(cp);
     th[2 * k] = th[2 * k + 1] = cp;
   }
+  // Instances are split into classes by neighbor count (m <= 16 or <= 32) and by correlation
+  // code -- the model, with Matern needing the general-nu kernel when nu is sampled or starts
+  // off the half-integers -- so each class runs the kernel instantiation it needs and no other.
+  constexpr int NCLS = 10;
+  std::vector<int> cls(ninst), pos(ninst);
+  std::vector<std::vector<BFData>> cdatas(NCLS);
+  std::vector<std::vector<PassEval>> cevCand(NCLS), cevCur(NCLS);
+  for (int k = 0; k < ninst; k++) {
+    const MCInstance &I = insts[k];
+    const bool gen = I.model == 2 && (I.tuning[3] != 0.0 || th[2 * k].halfk < 0);
+    const int cov = gen ? NNGP_COV_ANY : I.model;
+    cls[k] = (I.m <= 16 ? 0 : 5) + cov;
+    pos[k] = (int)cdatas[cls[k]].size();
+    cdatas[cls[k]].push_back(datas[k]);
+    cevCand[cls[k]].push_back(PassEval{pos[k], 2 * k + 1});
+    cevCur[cls[k]].push_back(PassEval{pos[k], 2 * k});
+  }
+  double *d_outc[NCLS] = {}, *d_out0c[NCLS] = {};
+  for (int c = 0; c < NCLS; c++) {
+    const size_t cnt = cdatas[c].size();
+    if (!cnt) continue;
+    d_outc[c] = (double *)own(sizeof(double) * 2 * cnt * ng);
+    d_out0c[c] = (double *)own(sizeof(double) * 2 * cnt);
+    if (!d_outc[c] || !d_out0c[c]) {
+      release();
+      return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+    }
+  }
+  for (int k = 0; k < ninst; k++) consts[k].out = d_outc[cls[k]] + (size_t)pos[k] * ng;
   MCConst *d_c = (MCConst *)own(sizeof(MCConst) * ninst);
   MCState *d_s = (MCState *)own(sizeof(MCState) * ninst);
   CovParams *d_th = (CovParams *)own(sizeof(CovParams) * 2 * ninst);
-  double *d_out = (double *)own(sizeof(double) * 2 * (size_t)ninst * ng);
-  double *d_out0 = (double *)own(sizeof(double) * 2 * (size_t)ninst);
   unsigned long long *d_status = (unsigned long long *)own(sizeof(unsigned long long));
-  if (!d_c || !d_s || !d_th || !d_out || !d_out0 || !d_status) {
+  if (!d_c || !d_s || !d_th || !d_status) {
     release();
     return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
   }
@@ -390,40 +407,64 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     release();
     return st;
   }
-  // plans: fused pass at each instance's candidate slot; standalone pass at the current slot
-  std::vector<PassEval> evCand(ninst), evCur(ninst);
-  for (int k = 0; k < ninst; k++) {
-    evCand[k] = PassEval{k, 2 * k + 1};
-    evCur[k] = PassEval{k, 2 * k};
+  BFPlan planCand[NCLS], planCur[NCLS];
+  bool haveCand[NCLS] = {}, haveCur[NCLS] = {};
+  auto free_plans = [&]() {
+    for (int c = 0; c < NCLS; c++) {
+      if (haveCand[c]) nngp_bf_plan_free(ctx, &planCand[c]);
+      if (haveCur[c]) nngp_bf_plan_free(ctx, &planCur[c]);
+    }
+  };
+  for (int c = 0; c < NCLS && !st; c++) {
+    if (cdatas[c].empty()) continue;
+    const int cov = c % 5;
+    st = nngp_bf_plan(ctx, &planCand[c], precision, 1, nv, cdatas[c], d_th, cevCand[c], d_status, cov);
+    haveCand[c] = true;
+    if (!st && anyRep) {
+      st = nngp_bf_plan(ctx, &planCur[c], precision, 0, 0, cdatas[c], d_th, cevCur[c], d_status, cov);
+      haveCur[c] = true;
+    }
   }
-  BFPlan planCand, planCur;
-  if ((st = nngp_bf_plan(ctx, &planCand, precision, 1, nv, datas, d_th, evCand, d_status))) {
+  if (st) {
+    free_plans();
     release();
     return st;
   }
-  if (anyRep && (st = nngp_bf_plan(ctx, &planCur, precision, 0, 0, datas, d_th, evCur, d_status))) {
-    nngp_bf_plan_free(ctx, &planCand);
-    release();
-    return st;
-  }
+  auto run_cand = [&]() -> int {
+    for (int c = 0; c < NCLS; c++)
+      if (haveCand[c]) {
+        const int r = nngp_bf_run(ctx, &planCand[c], d_outc[c]);
+        if (r) return r;
+      }
+    return NNGP_OK;
+  };
+  auto run_cur = [&]() -> int {
+    for (int c = 0; c < NCLS; c++)
+      if (haveCur[c]) {
+        const int r = nngp_bf_run(ctx, &planCur[c], d_out0c[c]);
+        if (r) return r;
+      }
+    return NNGP_OK;
+  };
   // initial state: likelihood pass at the starting theta (candidate slot = start)
-  st = nngp_bf_run(ctx, &planCand, d_out);
+  st = run_cand();
   if (!st) {
-    mc_init_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_out, ng, ninst);
+    mc_init_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
     ctx->launches++;
   }
   // one iteration as a graph (with and without the replicate draw)
   auto capture = [&](bool rep, cudaGraphExec_t *exec) -> int {
     cudaGraph_t g;
-    MC_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t eb = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (eb != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(eb));
     int s2 = NNGP_OK;
     mc_pre_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
     if (rep) {
-      s2 = nngp_bf_run(ctx, &planCur, d_out0);
+      s2 = run_cur();
       mc_rep_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
     }
-    if (!s2) s2 = nngp_bf_run(ctx, &planCand, d_out);
-    mc_post_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, d_out, ng, ninst);
+    if (!s2) s2 = run_cand();
+    mc_post_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (s2) return s2;
     if (e != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -433,6 +474,8 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     return NNGP_OK;
   };
   cudaGraphExec_t gPlain = nullptr, gRep = nullptr;
+  const bool timing = ctx->timing;
+  ctx->timing = false;  // no per-pass events inside a captured graph
   const int64_t launches_before = ctx->launches;
   if (!st) st = capture(false, &gPlain);
   const int64_t per_plain = ctx->launches - launches_before;
@@ -443,6 +486,7 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     per_rep = ctx->launches - b;
   }
   ctx->launches = launches_before;  // captured launches are counted when replayed below
+  ctx->timing = timing;
   for (int s = 0; !st && s < nS; s++) {
     const bool rep = anyRep && (*host_rep)[s] != 0;
     cudaError_t e = cudaGraphLaunch(rep ? gRep : gPlain, ctx->stream);
@@ -464,8 +508,7 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
       if (states[k].status == 3) st = nngp_fail(ctx, NNGP_ERR_STREAM, "rNNGP: a host-fed random stream ran out");
     }
   }
-  nngp_bf_plan_free(ctx, &planCand);
-  if (anyRep) nngp_bf_plan_free(ctx, &planCur);
+  free_plans();
   release();
   cudaStreamSynchronize(ctx->stream);
 #undef MC_TRY
@@ -549,6 +592,100 @@ extern "C" int nngp_rNNGP(nngp_ctx *ctx, const double *y, const double *X, int p
                   ctx->stream);
   if (nRep > 0 && repSamples)
     cudaMemcpyAsync(repSamples, I.repOut, sizeof(double) * (size_t)n * nRep, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fin(nngp_fail(ctx, NNGP_ERR_CUDA, cudaGetErrorString(e)));
+  return fin(NNGP_OK);
+}
+
+extern "C" int nngp_rNNGP_batch(nngp_ctx *ctx, int nprob, nngp_mcmc_problem *probs, int p, int precision,
+                                int resident) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (nprob < 0 || (nprob > 0 && !probs)) return nngp_fail(ctx, NNGP_ERR_ARG, "nprob >= 0 and probs required");
+  if (p < 1 || p > PMAX) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= p <= 7 required");
+  if (precision != NNGP_FP64 && precision != NNGP_FP32R) return nngp_fail(ctx, NNGP_ERR_ARG, "unknown precision");
+  for (int k = 0; k < nprob; k++) {
+    const nngp_mcmc_problem &P = probs[k];
+    if (P.n < 1 || P.m < 1 || P.m > NNGP_MAX_M || P.n < P.m)
+      return nngp_fail(ctx, NNGP_ERR_ARG, "n >= m and 1 <= m <= 32 required in every chain");
+    if (P.covModel < 0 || P.covModel > 3) return nngp_fail(ctx, NNGP_ERR_ARG, "cov.model is not correctly specified");
+    if (P.nSamples < 0) return nngp_fail(ctx, NNGP_ERR_ARG, "n.samples must be >= 0");
+    if (!P.sigmaSqIG || !P.tauSqIG || !P.phiUnif || (P.covModel == 2 && !P.nuUnif) || !P.betaStarting ||
+        !P.thetaStarting || !P.tuning)
+      return nngp_fail(ctx, NNGP_ERR_ARG, "priors, starting values and tuning are required");
+  }
+  if (nprob == 0) return NNGP_OK;
+  cudaSetDevice(ctx->device);
+  std::vector<void *> tmp;
+  auto up = [&](const void *h, size_t bytes) -> void * {
+    if (resident) return const_cast<void *>(h);
+    void *d = nngp_malloc_async(ctx, bytes ? bytes : 16);
+    if (d && bytes && h) cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    tmp.push_back(d);
+    return d;
+  };
+  auto fin = [&](int status) {
+    for (void *q : tmp) nngp_free_async(ctx, q);
+    cudaStreamSynchronize(ctx->stream);
+    return status;
+  };
+  std::vector<MCInstance> insts;
+  std::vector<int> which;
+  for (int k = 0; k < nprob; k++) {
+    nngp_mcmc_problem &P = probs[k];
+    P.nAccept = 0;
+    if (P.nSamples == 0) continue;
+    const int n = P.n, m = P.m, nTheta = P.covModel == 2 ? 4 : 3;
+    const int64_t nI = nngp_nindx(n, m);
+    MCInstance I{};
+    I.n = n;
+    I.m = m;
+    I.p = p;
+    I.model = P.covModel;
+    I.coords_cm = (const double *)up(P.coords, sizeof(double) * 2 * n);
+    I.nnIndx = (const int *)up(P.nnIndx, sizeof(int) * (nI > 0 ? nI : 0));
+    I.nnLU = (const int *)up(P.nnIndxLU, sizeof(int) * 2 * n);
+    I.X = (const double *)up(P.X, sizeof(double) * (size_t)n * p);
+    I.y = (const double *)up(P.y, sizeof(double) * n);
+    for (int t = 0; t < 2; t++) {
+      I.sIG[t] = P.sigmaSqIG[t];
+      I.tIG[t] = P.tauSqIG[t];
+      I.pU[t] = P.phiUnif[t];
+      I.nU[t] = P.covModel == 2 ? P.nuUnif[t] : 0.0;
+    }
+    for (int t = 0; t < p; t++) I.betaStart[t] = P.betaStarting[t];
+    for (int t = 0; t < 4; t++) {
+      I.thetaStart[t] = t < nTheta ? P.thetaStarting[t] : 0.0;
+      I.tuning[t] = t < nTheta ? P.tuning[t] : 0.0;
+    }
+    I.nSamples = P.nSamples;
+    I.normals = (const double *)up(P.normals, sizeof(double) * (size_t)P.nNormals);
+    I.nNormals = P.nNormals;
+    I.unifs = (const double *)up(P.unifs, sizeof(double) * (size_t)P.nUnifs);
+    I.nUnifs = P.nUnifs;
+    I.repIndx = nullptr;
+    I.betaOut = resident ? P.betaSamples : (double *)up(nullptr, sizeof(double) * (size_t)p * P.nSamples);
+    I.thetaOut = resident ? P.thetaSamples : (double *)up(nullptr, sizeof(double) * (size_t)nTheta * P.nSamples);
+    I.repOut = nullptr;
+    insts.push_back(I);
+    which.push_back(k);
+  }
+  for (void *q : tmp)
+    if (!q) return fin(nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed"));
+  if (insts.empty()) return fin(NNGP_OK);
+  std::vector<int> acc(insts.size(), 0);
+  int st = nngp_run_mcmc(ctx, insts, precision, nullptr, acc.data());
+  if (st) return fin(st);
+  for (size_t j = 0; j < insts.size(); j++) {
+    nngp_mcmc_problem &P = probs[which[j]];
+    P.nAccept = acc[j];
+    if (!resident) {
+      const int nTheta = P.covModel == 2 ? 4 : 3;
+      cudaMemcpyAsync(P.betaSamples, insts[j].betaOut, sizeof(double) * (size_t)p * P.nSamples,
+                      cudaMemcpyDeviceToHost, ctx->stream);
+      cudaMemcpyAsync(P.thetaSamples, insts[j].thetaOut, sizeof(double) * (size_t)nTheta * P.nSamples,
+                      cudaMemcpyDeviceToHost, ctx->stream);
+    }
+  }
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return fin(nngp_fail(ctx, NNGP_ERR_CUDA, cudaGetErrorString(e)));
   return fin(NNGP_OK);

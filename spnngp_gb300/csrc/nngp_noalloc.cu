@@ -27,11 +27,6 @@
 #include <string>
 #include "nngp_internal.h"
 
-namespace nngp_bf {
-template <int M, bool R32, int MODE>
-int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass);
-}
-
 namespace {
 
 constexpr int kMaxN = 65536;
@@ -205,8 +200,8 @@ extern "C" int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, cons
     return report(fail(&ctx, NNGP_ERR_CUDA, (std::string("nngp_loglik_gram_noalloc: ") + cudaGetErrorString(e)).c_str()));
   na_interleave_kernel<<<(n + 255) / 256, 256, 0, ctx.stream>>>(coords, n, xy);
   na_row_major_kernel<<<(unsigned)(((long)n * nv + 255) / 256), 256, 0, ctx.stream>>>(V, n, nv, Vrm);
-  st = m <= 16 ? nngp_bf::launch_one<16, false, 1>(&ctx, &plan, false)
-               : nngp_bf::launch_one<32, false, 1>(&ctx, &plan, false);
+  plan.cov = nngp_plan_cov(&cp, 1);
+  st = nngp_bf_launch(&ctx, &plan, false, false);
   if (st) return report(st);
   na_finish_kernel<<<1, 256, 0, ctx.stream>>>(partial, job.ntiles, nv, logDet, gram);
   e = cudaGetLastError();

@@ -43,3 +43,22 @@ def test_missing_library_fails_loudly(tmp_path):
 
     with pytest.raises(ImportError):
         _lib._Lib(str(tmp_path / "nope.so"))
+
+
+def declared_arity():
+    text = open(HEADER).read()
+    out = {}
+    for m in re.finditer(r"\b(nngp_[A-Za-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_python_bindings_match_header():
+    """Every ctypes signature names a declared entry point with the declared number of arguments."""
+    from spnngp_gb300._lib import _SIGNATURES
+
+    arity = declared_arity()
+    for name, (_, argtypes) in _SIGNATURES.items():
+        assert name in arity, name
+        assert len(argtypes) == arity[name], (name, len(argtypes), arity[name])

@@ -139,3 +139,83 @@ def test_cNNGP_many_grid_points_match_oracle(sp, orc):
     assert np.max(np.abs(rg["beta.hat"] - ro["beta"])) <= 1e-9
     assert np.max(np.abs(rg["y.0.hat"] - ro["y0"])) <= 1e-9
     assert np.max(np.abs(rg["y.0.hat.var"] - ro["y0var"]) / ro["y0var"]) <= 1e-9
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32r", 1e-6)])
+def test_cNNGP_multi_matches_single_problem_runs(sp, orc, precision, tol):
+    from spnngp_gb300 import api
+
+    rng = np.random.default_rng(41)
+    problems, singles = [], []
+    ta = np.array([[phi, a] for phi in (3.0, 9.0, 25.0) for a in (0.1, 0.8)]).T
+    for k, n in enumerate((1200, 2500, 1800)):  # uneven folds
+        c = xorder(rng.uniform(size=(n, 2)))
+        X = np.column_stack([np.ones(n), rng.normal(size=n)])
+        y = X @ [1.0, -0.5] + rng.normal(size=n)
+        n0 = 150 + 40 * k
+        c0 = rng.uniform(size=(n0, 2))
+        X0 = np.column_stack([np.ones(n0), rng.normal(size=n0)])
+        y0 = X0 @ [1.0, -0.5] + rng.normal(size=n0)
+        o = orc.mkNNIndxCB(cm(c), 12)
+        nn0, _ = orc.nn2(c, c0, 12)
+        P = {"y": y, "X": X, "coords": c, "nn_indx": o[0], "nn_indx_lu": o[2], "theta_alpha": ta, "X0": X0,
+             "coords0": c0, "nn_indx0": nn0, "y0_true": y0}
+        problems.append(P)
+        singles.append(sp.cNNGP(y, X, c, ta, o[0], o[2], X0, c0, nn0, 12, [2, 1], "exponential",
+                                precision=precision))
+    outs = sp.cNNGP_multi(problems, 12, [2, 1], "exponential", precision=precision)
+    for P, o, s in zip(problems, outs, singles):
+        for k in ("beta.hat", "ab", "bb", "y.0.hat", "y.0.hat.var"):
+            assert np.allclose(o[k], s[k], rtol=tol, atol=tol), k
+        for j in range(ta.shape[1]):
+            assert o["crps"][j] == pytest.approx(api.crps(P["y0_true"], s["y.0.hat"][:, j], s["y.0.hat.var"][:, j]),
+                                                 rel=1e-9)
+            assert o["rmspe"][j] == pytest.approx(api.rmspe(P["y0_true"], s["y.0.hat"][:, j]), rel=1e-9)
+
+
+def _chain(sp, rng, n, m, model, nS, p=2):
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n)] + [rng.normal(size=n) for _ in range(p - 1)])
+    y = X @ np.linspace(1.0, -0.5, p) + rng.normal(size=n)
+    knn = sp.mkNNIndxCB(c, m)
+    nn, lu = knn["nnIndx"], knn["nnIndxLU"]
+    nTheta = 4 if model == 2 else 3
+    return {"y": y, "X": X, "coords": c, "nn_indx": nn, "nn_indx_lu": lu, "m": m, "cov_model": model,
+            "sigma_sq_IG": [2, 1], "tau_sq_IG": [2, 0.1], "phi_unif": [3, 30], "nu_unif": [0.2, 2.0],
+            "beta_starting": np.linspace(1.0, -0.5, p), "theta_starting": [1.0, 0.2, 6.0, 0.8][:nTheta],
+            "tuning": [0.1, 0.1, 0.4, 0.1][:nTheta], "n_samples": nS,
+            "normals": rng.normal(size=nS * (p + nTheta) + 5), "unifs": rng.uniform(size=nS + 1)}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32r"])
+def test_rNNGP_batch_same_as_each_chain_alone(sp, precision):
+    """Chains of uneven size, both neighbor classes and all four models, advanced together, give
+    exactly the draws each gives alone."""
+    rng = np.random.default_rng(31)
+    specs = [(700, 10, 0, 40), (1800, 15, 1, 25), (450, 20, 2, 30), (1200, 32, 3, 40), (900, 5, 0, 0),
+             (2500, 16, 2, 35)]
+    chains = [_chain(sp, rng, *s) for s in specs]
+    batch = sp.rNNGP_batch(chains, precision=precision)
+    for P, r in zip(chains, batch):
+        if P["n_samples"] == 0:
+            assert r["accept"] == 0 and r["p.theta.samples"].size == 0
+            continue
+        a = sp.rNNGP(P["y"], P["X"], P["m"], P["coords"], P["cov_model"], P["nn_indx"], P["nn_indx_lu"],
+                     P["sigma_sq_IG"], P["tau_sq_IG"], P["phi_unif"], P["nu_unif"] if P["cov_model"] == 2 else None,
+                     P["beta_starting"], P["theta_starting"], P["tuning"], P["n_samples"], P["normals"], P["unifs"],
+                     precision=precision)
+        assert r["accept"] == a["accept"]
+        assert np.array_equal(r["p.theta.samples"], a["p.theta.samples"])
+        assert np.array_equal(r["p.beta.samples"], a["p.beta.samples"])
+
+
+def test_rNNGP_batch_matches_oracle(sp, orc):
+    rng = np.random.default_rng(32)
+    chains = [_chain(sp, rng, 800, 12, 0, 60), _chain(sp, rng, 600, 20, 3, 60)]
+    batch = sp.rNNGP_batch(chains)
+    for P, r in zip(chains, batch):
+        ro = orc.rNNGP(P["y"], cm(P["X"]), P["m"], cm(P["coords"]), P["cov_model"], P["nn_indx"], P["nn_indx_lu"],
+                       P["sigma_sq_IG"], P["tau_sq_IG"], P["phi_unif"], [0, 0], P["beta_starting"],
+                       P["theta_starting"], P["tuning"], P["n_samples"], P["normals"], P["unifs"])
+        assert r["accept"] == ro["accept"]
+        assert np.max(np.abs(r["p.theta.samples"] - ro["theta"]) / ro["theta"]) <= TOL
