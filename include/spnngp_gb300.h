@@ -259,6 +259,24 @@ int nngp_measure_peak(nngp_ctx *ctx, int fp64, double *flops_per_s);
 int nngp_set_kernel_timing(nngp_ctx *ctx, int on);
 int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches);
 
+/* Launch-shape autotuner of the FP32R B/F kernel for m <= 16, no counterpart
+ * in the reference (it stands in for the reference's n.omp.threads tuning).
+ * The first pass of a (neighbor bound, mode, correlation model, size class)
+ * times every candidate shape -- warps per block 1/2/4/8 x one tile per warp
+ * or a persistent grid of 1 or 2 x resident blocks x SMs -- on the caller's
+ * own data and keeps the fastest for the context; passes under stream capture
+ * use the tuned shape, or the default (4 warps, one tile per warp) when none is
+ * tuned yet.  Results are identical for every shape (each warp reduces its own
+ * 32 locations and the sums are combined in a fixed order), so tuning never
+ * changes a result.  nngp_set_autotune(ctx, 0) turns tuning off (default
+ * shape); nngp_set_launch_shape forces a shape (wpb 0 = back to tuning);
+ * nngp_autotune_report writes one line per tuned class ("key: wpb=W grid_mode=G
+ * ms=T | WxBLOCKS:ms WxBLOCKS:ms ...", one entry per candidate shape) into buf
+ * and returns the number of classes. */
+int nngp_set_autotune(nngp_ctx *ctx, int on);
+int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode);
+int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len);
+
 /* No counterpart in the reference.  The FP64 fused likelihood pass of
  * nngp_loglik_gram_dev for callers that cannot allocate device memory when they
  * need it (a host whose allocator owns all device memory, a serving process that

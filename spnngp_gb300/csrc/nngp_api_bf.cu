@@ -7,12 +7,18 @@
 
 namespace {
 
-// col-major n x nv -> row-major n x nv
-__global__ void to_row_major_kernel(const double *__restrict__ cm, int n, int nv, double *__restrict__ rm) {
+// col-major n x nv -> row-major n x nv, and (when rmf is given) its float (hi, lo) split
+__global__ void to_row_major_kernel(const double *__restrict__ cm, int n, int nv, double *__restrict__ rm,
+                                    float2 *__restrict__ rmf) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long)n * nv) {
     const int i = (int)(t / nv), v = (int)(t % nv);
-    rm[t] = cm[(size_t)v * n + i];
+    const double x = cm[(size_t)v * n + i];
+    rm[t] = x;
+    if (rmf) {
+      const float h = (float)x;
+      rmf[t] = make_float2(h, (float)(x - (double)h));
+    }
   }
 }
 
@@ -86,14 +92,18 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
     return nngp_fail(ctx, NNGP_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32R)");
   double *xy, *Vrm = nullptr;
   float *xyf = nullptr;
+  float2 *Vf = nullptr;
   NNGP_ALLOC(ctx, xy, double, S_COORDS, 2 * (size_t)n);
   if (precision == NNGP_FP32R) NNGP_ALLOC(ctx, xyf, float, S_XYF, 4 * (size_t)n);
   int st0 = nngp_prepare_coords(ctx, d_coords_cm, n, xy, xyf);
   if (st0) return st0;
   if (mode == 1) {
     NNGP_ALLOC(ctx, Vrm, double, S_V, (size_t)n * nv);
+    // V changes from call to call under a cached plan: the register kernel's float split is
+    // refreshed here rather than by the plan
+    if (nngp_reg_m(precision, m) > 0) NNGP_ALLOC(ctx, Vf, float2, S_VF, (size_t)n * nv);
     const long tot = (long)n * nv;
-    to_row_major_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(d_V_cm, n, nv, Vrm);
+    to_row_major_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(d_V_cm, n, nv, Vrm, Vf);
     NNGP_LAUNCH_CHECK(ctx);
   }
   CovParams *d_theta;
@@ -115,11 +125,12 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   d.nnIndx = d_nnIndx;
   d.nnLU = d_nnLU;
   d.V = Vrm;
+  d.Vf = Vf;
   d.B = d_B;
   d.F = d_F;
-  char key[256];
-  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p/%p", nngp_plan_cov(&cp, 1), mode, precision, n, m, nv, (const void *)xy,
-           (const void *)xyf,
+  char key[512];
+  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p/%p/%p/%p/%p", nngp_plan_cov(&cp, 1), mode, precision, n, m, nv, (const void *)xy,
+           (const void *)xyf, (const void *)Vf,
            (const void *)d_nnIndx, (const void *)d_nnLU, (const void *)Vrm, (void *)d_B, (void *)d_F,
            (void *)d_theta, (void *)d_status);
   if (!ctx->cache_plan || ctx->cache_key != key) {

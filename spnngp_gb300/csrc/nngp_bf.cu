@@ -1,11 +1,15 @@
 #include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
 #include <type_traits>
 #include "nngp_internal.h"
 
 // Host side of the B/F pass: plans (job tables), dispatch to the kernel
-// instantiations of nngp_bf_inst.cu (one object per neighbor bound, precision and
-// correlation code), and the fixed-order reductions.  The kernel itself is
-// documented in nngp_bf_kernel.cuh.
+// instantiations (nngp_bf_inst.cu: the shared-memory kernels, one object per
+// neighbor bound, precision and correlation code; nngp_bfr_inst.cu: the
+// register FP32R kernel for m <= 16), the autotuner of the register kernel's
+// launch shape, and the fixed-order reductions.  The kernels are documented in
+// nngp_bf_kernel.cuh and nngp_bfr_kernel.cuh.
 namespace nngp_bf {
 template <int M, bool R32, int MODE, int COV>
 int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass);
@@ -14,25 +18,47 @@ constexpr int bf_tpb() {
   return R32 ? (M <= 16 ? 128 : 64) : (M <= 16 ? 64 : 32);
 }
 }  // namespace nngp_bf
+namespace nngp_bfr {
+template <int M, int MODE, int COV>
+int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid);
+template <int M, int MODE, int COV>
+int occupancy(int wpb);
+}  // namespace nngp_bfr
 using namespace nngp_bf;
 
 namespace {
-// Fixed-order reduction of per-tile partials: block `job`, value v.
-__global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, int ng,
+// Sum over the 256 threads of a block, in a fixed tree order (every thread gets the sum).
+__device__ double block_sum256(double x, double *sbuf) {
+  sbuf[threadIdx.x] = x;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sbuf[threadIdx.x] += sbuf[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double r = sbuf[0];
+  __syncthreads();
+  return r;
+}
+
+// Fixed-order reduction of per-tile partials: block `job`, value v.  With jobs_fb, the FP64
+// re-solve's partials of the tiles marked in fb_marks are added (also in tile order).
+__global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, const BFJob *__restrict__ jobs_fb,
+                                       const unsigned *__restrict__ fb_marks, int ng,
                                        double *__restrict__ out) {
   const BFJob job = jobs[blockIdx.x];
   __shared__ double sbuf[256];
   for (int v = 0; v < ng; v++) {
     double s = 0.0;
     for (int t = threadIdx.x; t < job.ntiles; t += 256) s += job.partial[(size_t)t * ng + v];
-    sbuf[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (threadIdx.x < w) sbuf[threadIdx.x] += sbuf[threadIdx.x + w];
-      __syncthreads();
+    s = block_sum256(s, sbuf);
+    if (jobs_fb) {
+      const BFJob jf = jobs_fb[blockIdx.x];
+      double f = 0.0;
+      for (int t = threadIdx.x; t < jf.ntiles; t += 256)
+        if (fb_marks[jf.tile0 + t]) f += jf.partial[(size_t)t * ng + v];
+      s += block_sum256(f, sbuf);
     }
-    if (threadIdx.x == 0) out[(size_t)blockIdx.x * ng + v] = sbuf[0];
-    __syncthreads();
+    if (threadIdx.x == 0) out[(size_t)blockIdx.x * ng + v] = s;
   }
 }
 
@@ -41,9 +67,9 @@ __global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, int ng,
 namespace {
 template <int MODE, int COV>
 int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
-  if (pl->mmax <= 16)
-    return fp32r ? launch_one<16, true, MODE, COV>(ctx, pl, fallback_pass)
-                 : launch_one<16, false, MODE, COV>(ctx, pl, fallback_pass);
+  // FP32R with m <= 16 runs the register kernel (launched by run_reg); the FP64
+  // re-solve of its flagged locations lands here with fp32r false
+  if (pl->mmax <= 16) return launch_one<16, false, MODE, COV>(ctx, pl, fallback_pass);
   return fp32r ? launch_one<32, true, MODE, COV>(ctx, pl, fallback_pass)
                : launch_one<32, false, MODE, COV>(ctx, pl, fallback_pass);
 }
@@ -59,20 +85,137 @@ int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass)
   }
 }
 
-int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
-  return pl->mode == 0 ? launch_mode<0>(ctx, pl, fp32r, fallback_pass)
-                       : launch_mode<1>(ctx, pl, fp32r, fallback_pass);
+// ---------------------------------------------------------------- register kernel
+// Calls launch_reg (query_occ false) or occupancy (true) of the plan's instantiation.
+template <int M, int MODE>
+int reg_call_m(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ) {
+  using namespace nngp_bfr;
+  switch (pl->cov) {
+    case NNGP_COV_EXP:
+      return query_occ ? occupancy<M, MODE, NNGP_COV_EXP>(wpb) : launch_reg<M, MODE, NNGP_COV_EXP>(ctx, pl, wpb, grid);
+    case NNGP_COV_SPH:
+      return query_occ ? occupancy<M, MODE, NNGP_COV_SPH>(wpb) : launch_reg<M, MODE, NNGP_COV_SPH>(ctx, pl, wpb, grid);
+    case NNGP_COV_MAT_HALF:
+      return query_occ ? occupancy<M, MODE, NNGP_COV_MAT_HALF>(wpb)
+                       : launch_reg<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, wpb, grid);
+    case NNGP_COV_GAU:
+      return query_occ ? occupancy<M, MODE, NNGP_COV_GAU>(wpb) : launch_reg<M, MODE, NNGP_COV_GAU>(ctx, pl, wpb, grid);
+    default:
+      return query_occ ? occupancy<M, MODE, NNGP_COV_ANY>(wpb) : launch_reg<M, MODE, NNGP_COV_ANY>(ctx, pl, wpb, grid);
+  }
+}
+int reg_call(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ) {
+  const bool m1 = pl->mode == 1;
+  switch (pl->reg_m) {
+    case 10: return m1 ? reg_call_m<10, 1>(ctx, pl, wpb, grid, query_occ) : reg_call_m<10, 0>(ctx, pl, wpb, grid, query_occ);
+    case 15: return m1 ? reg_call_m<15, 1>(ctx, pl, wpb, grid, query_occ) : reg_call_m<15, 0>(ctx, pl, wpb, grid, query_occ);
+    default: return m1 ? reg_call_m<16, 1>(ctx, pl, wpb, grid, query_occ) : reg_call_m<16, 0>(ctx, pl, wpb, grid, query_occ);
+  }
 }
 
-__global__ void add_into_kernel(double *__restrict__ dst, const double *__restrict__ src, int count) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < count) dst[t] += src[t];
+// Blocks of the launch shape (wpb, grid_mode) for this plan: grid_mode 0 gives every warp one
+// tile; k > 0 caps the grid at k x (resident blocks per SM) x SMs, each warp looping over tiles.
+int reg_grid(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid_mode) {
+  const int full = (pl->tiles + wpb - 1) / wpb;
+  if (grid_mode <= 0) return full > 0 ? full : 1;
+  const int occ = reg_call(ctx, pl, wpb, 0, true);
+  const long cap = (long)grid_mode * occ * (ctx->sm_count > 0 ? ctx->sm_count : 1);
+  return (int)(cap < full ? cap : full);
+}
+
+std::string tune_key(const BFPlan *pl) {
+  int bucket = 0;
+  while ((1 << (bucket + 1)) <= pl->tiles) bucket++;
+  char k[96];
+  snprintf(k, sizeof k, "M=%d mode=%d cov=%d tiles~2^%d", pl->reg_m, pl->mode, pl->cov, bucket);
+  return k;
+}
+
+// Times every candidate shape on the plan itself (each run rewrites the same outputs with
+// the same values: the results do not depend on the shape) and keeps the fastest.
+int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best) {
+  static const int kWpb[] = {1, 2, 3, 4, 5, 6, 8};
+  static const int kGrid[] = {0, 1, 2};
+  cudaEvent_t e0, e1;
+  NNGP_CUDA_TRY(ctx, cudaEventCreate(&e0));
+  NNGP_CUDA_TRY(ctx, cudaEventCreate(&e1));
+  best = TuneEntry();
+  best.ms = 1e30;
+  std::string detail;
+  int st = NNGP_OK;
+  for (int wpb : kWpb) {
+    if (wpb > nngp_bfr_max_wpb(pl->reg_m)) continue;
+    const int full = reg_grid(ctx, pl, wpb, 0);
+    for (int gm : kGrid) {
+      const int grid = reg_grid(ctx, pl, wpb, gm);
+      if (gm > 0 && grid >= full) continue;  // same as the one-tile-per-warp grid
+      if ((st = reg_call(ctx, pl, wpb, grid, false))) break;  // warm-up
+      cudaEventRecord(e0, ctx->stream);
+      if ((st = reg_call(ctx, pl, wpb, grid, false))) break;
+      cudaEventRecord(e1, ctx->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        st = nngp_fail(ctx, NNGP_ERR_CUDA, "autotune: event synchronisation failed");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      char buf[64];
+      snprintf(buf, sizeof buf, "%s%dx%d:%.4f", detail.empty() ? "" : " ", wpb, grid, ms);
+      detail += buf;
+      if (ms < best.ms) {
+        best.ms = ms;
+        best.wpb = wpb;
+        best.grid_mode = gm;
+      }
+    }
+    if (st) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  best.detail = detail;
+  return st;
+}
+
+int run_reg(nngp_ctx *ctx, const BFPlan *pl) {
+  int wpb = 4, gm = 0;
+  if (ctx->force_wpb > 0) {
+    wpb = ctx->force_wpb;
+    gm = ctx->force_grid_mode;
+  } else {
+    const std::string key = tune_key(pl);
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) {
+      wpb = it->second.wpb;
+      gm = it->second.grid_mode;
+    } else if (ctx->autotune) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      cudaStreamIsCapturing(ctx->stream, &cs);
+      if (cs == cudaStreamCaptureStatusNone) {
+        TuneEntry e;
+        const int st = tune_reg(ctx, pl, e);
+        if (st) return st;
+        ctx->tuned[key] = e;
+        wpb = e.wpb;
+        gm = e.grid_mode;
+      }
+    }
+  }
+  const int wmax = nngp_bfr_max_wpb(pl->reg_m);
+  if (wpb > wmax) wpb = wmax;  // a forced shape larger than the block limit of this bound
+  return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm), false);
+}
+
+int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
+  if (fp32r && !fallback_pass && pl->reg_m > 0) return run_reg(ctx, pl);
+  return pl->mode == 0 ? launch_mode<0>(ctx, pl, fp32r, fallback_pass)
+                       : launch_mode<1>(ctx, pl, fp32r, fallback_pass);
 }
 
 }  // namespace
 
 int nngp_bf_tile(int precision, int mmax) {
-  if (precision == NNGP_FP32R) return mmax <= 16 ? bf_tpb<16, true>() : bf_tpb<32, true>();
+  if (nngp_reg_m(precision, mmax) > 0) return 32;  // the register kernel's tiles are warps
+  if (precision == NNGP_FP32R) return bf_tpb<32, true>();
   return mmax <= 16 ? bf_tpb<16, false>() : bf_tpb<32, false>();
 }
 
@@ -120,6 +263,7 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
   for (const BFData &d : datas) mmax = d.m > mmax ? d.m : mmax;
   pl->mmax = mmax;
   if (mmax > NNGP_MAX_M) return nngp_fail(ctx, NNGP_ERR_ARG, "m exceeds the supported maximum (32)");
+  pl->reg_m = nngp_reg_m(precision, mmax);
   if (pl->nv > NNGP_MAX_NV) return nngp_fail(ctx, NNGP_ERR_ARG, "too many columns in the fused pass (max 8)");
   auto own = [&](size_t bytes) -> void * {
     void *p = nngp_malloc_async(ctx, bytes);
@@ -135,6 +279,9 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
   if (precision == NNGP_FP32R) {
     build_jobs(nngp_bf_tile(NNGP_FP64, mmax), datas, evals, pl->ng, jobs_fb, pe_fb, pl->tiles_fb);
     pl->d_partial_fb = (double *)own(sizeof(double) * pe_fb);
+    pl->d_fb_words = (unsigned *)own(sizeof(unsigned) * (1 + (size_t)pl->tiles_fb));
+    pl->d_fb_list = (int *)own(sizeof(int) * (size_t)(pl->tiles_fb > 0 ? pl->tiles_fb : 1));
+    if (!pl->d_fb_words || !pl->d_fb_list) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
     size_t fb = 0;
     for (const PassEval &e : evals) fb += (size_t)datas[e.data].n;
     pl->flags_bytes = fb;
@@ -148,12 +295,30 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
       jobs_fb[k].partial = pl->d_partial_fb + reinterpret_cast<size_t>(jobs_fb[k].partial);
       jobs[k].flags = jobs_fb[k].flags = pl->d_flags + foff;
       foff += (size_t)datas[evals[k].data].n;
+      jobs[k].fb_tile0 = jobs_fb[k].tile0;
+      jobs[k].fb_tpb = nngp_bf_tile(NNGP_FP64, mmax);
+      jobs[k].fb_count = (int *)pl->d_fb_words;
+      jobs[k].fb_marks = pl->d_fb_words + 1;
+      jobs[k].fb_list = pl->d_fb_list;
+    }
+  }
+  // the register kernel reads V as float (hi, lo) pairs: split it once for callers that
+  // did not provide them (their V stays fixed for the plan's lifetime)
+  std::vector<BFData> dv(datas);
+  if (pl->reg_m > 0 && mode == 1) {
+    for (BFData &d : dv) {
+      if (d.Vf || !d.V) continue;
+      float2 *vf = (float2 *)own(sizeof(float2) * (size_t)d.n * nv);
+      if (!vf) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+      int st = nngp_split_v(ctx, d.V, (int64_t)d.n * nv, vf);
+      if (st) return st;
+      d.Vf = vf;
     }
   }
   pl->d_datas = (BFData *)own(sizeof(BFData) * datas.size());
   pl->d_jobs = (BFJob *)own(sizeof(BFJob) * jobs.size());
   if (!pl->d_datas || !pl->d_jobs) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(pl->d_datas, datas.data(), sizeof(BFData) * datas.size(),
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(pl->d_datas, dv.data(), sizeof(BFData) * dv.size(),
                                      cudaMemcpyHostToDevice, ctx->stream));
   NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(pl->d_jobs, jobs.data(), sizeof(BFJob) * jobs.size(),
                                      cudaMemcpyHostToDevice, ctx->stream));
@@ -171,7 +336,10 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
 int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   int st;
   const bool fp32r = pl->precision == NNGP_FP32R;
-  if (fp32r) NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_flags, 0, pl->flags_bytes, ctx->stream));
+  if (fp32r) {
+    NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_flags, 0, pl->flags_bytes, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_fb_words, 0, sizeof(unsigned) * (1 + (size_t)pl->tiles_fb), ctx->stream));
+  }
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   if (ctx->timing) {
     for (cudaEvent_t *e : {&t0, &t1}) {
@@ -189,18 +357,11 @@ int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
     cudaEventRecord(t1, ctx->stream);
     ctx->timed.emplace_back(t0, t1);
   }
-  reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(pl->d_jobs, pl->ng, d_out);
+  // FP32R: the FP64 re-solve of the recorded tiles, folded into the same fixed-order sums
+  if (fp32r && (st = launch_pass(ctx, pl, false, true))) return st;
+  reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr,
+                                                             fp32r ? pl->d_fb_words + 1 : nullptr, pl->ng, d_out);
   NNGP_LAUNCH_CHECK(ctx);
-  if (fp32r) {
-    // FP64 re-solve of the flagged locations, then fold its sums in
-    if ((st = launch_pass(ctx, pl, false, true))) return st;
-    double *tmp = d_out + (size_t)pl->njobs * pl->ng;  // caller provides 2 x njobs x ng
-    reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(pl->d_jobs_fb, pl->ng, tmp);
-    NNGP_LAUNCH_CHECK(ctx);
-    const int cnt = pl->njobs * pl->ng;
-    add_into_kernel<<<(cnt + 255) / 256, 256, 0, ctx->stream>>>(d_out, tmp, cnt);
-    NNGP_LAUNCH_CHECK(ctx);
-  }
   return NNGP_OK;
 }
 
@@ -223,6 +384,37 @@ void nngp_bf_cache_release(nngp_ctx *ctx) {
 }
 
 extern "C" {
+int nngp_set_autotune(nngp_ctx *ctx, int on) {
+  if (!ctx) return NNGP_ERR_ARG;
+  ctx->autotune = on != 0;
+  return NNGP_OK;
+}
+int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (warps_per_block < 0 || warps_per_block > 8 || grid_mode < 0 || grid_mode > 64)
+    return nngp_fail(ctx, NNGP_ERR_ARG, "launch shape: 0 <= warps_per_block <= 8, 0 <= grid_mode <= 64");
+  ctx->force_wpb = warps_per_block;
+  ctx->force_grid_mode = grid_mode;
+  return NNGP_OK;
+}
+int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len) {
+  if (!ctx) return NNGP_ERR_ARG;
+  std::string out;
+  for (const auto &kv : ctx->tuned) {
+    char line[160];
+    snprintf(line, sizeof line, "%s: wpb=%d grid_mode=%d ms=%.4f | ", kv.first.c_str(), kv.second.wpb,
+             kv.second.grid_mode, kv.second.ms);
+    out += line;
+    out += kv.second.detail;
+    out += "\n";
+  }
+  if (buf && len > 0) {
+    const size_t k = out.size() < (size_t)(len - 1) ? out.size() : (size_t)(len - 1);
+    memcpy(buf, out.data(), k);
+    buf[k] = 0;
+  }
+  return (int)ctx->tuned.size();
+}
 int nngp_set_kernel_timing(nngp_ctx *ctx, int on) {
   ctx->timing = on != 0;
   return NNGP_OK;
@@ -260,6 +452,24 @@ __global__ void prepare_coords_kernel(const double *__restrict__ cm, int n, doub
   }
 }
 }  // namespace
+
+namespace {
+__global__ void split_v_kernel(const double *__restrict__ V, int64_t count, float2 *__restrict__ Vf) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) {
+    const double v = V[t];
+    const float h = (float)v;
+    Vf[t] = make_float2(h, (float)(v - (double)h));
+  }
+}
+}  // namespace
+
+int nngp_split_v(nngp_ctx *ctx, const double *V, int64_t count, float2 *Vf) {
+  if (count <= 0) return NNGP_OK;
+  split_v_kernel<<<(unsigned)((count + 255) / 256), 256, 0, ctx->stream>>>(V, count, Vf);
+  NNGP_LAUNCH_CHECK(ctx);
+  return NNGP_OK;
+}
 
 int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf) {
   if (n <= 0) return NNGP_OK;

@@ -14,13 +14,15 @@
 //
 // Precision modes:
 //   FP64   everything in double.
-//   FP32R  coordinates differenced in FP64 and split into float hi/lo parts;
-//          covariance build, Cholesky and both triangular solves in float; then
-//          one refinement step: the residual c - C b is accumulated in FP64 (the
-//          float entries of C and b multiply exactly in double), the correction
-//          is solved with the float factor, and B = b + delta is kept in FP64.
+//   FP32R  (built for the 32-neighbor bound; m <= 16 runs the register kernel of
+//          nngp_bfr_kernel.cuh) coordinates split into float hi/lo parts and
+//          differenced exactly; covariance build, Cholesky and both triangular
+//          solves in float; then one refinement step: the residual c - C b of the
+//          float-evaluated C accumulated as a compensated (Dot2) float pair, the
+//          correction solved with the float factor, B = b + delta kept in FP64.
 //          F, log F and the Gram sums are FP64.  A location whose float pivot is
-//          not positive is flagged and re-solved by the FP64 kernel.
+//          not positive, or whose F is below 1e-3 (sigma^2 + tau^2), is flagged and
+//          re-solved by the FP64 kernel, which walks the list of flagged tiles.
 //
 // Modes: 0 writes B (packed, nIndx) and F and per-tile sums of log F;
 //        1 (fused likelihood) writes no B/F but per-tile sums of log F and of
@@ -108,7 +110,8 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
                                                  const BFJob *__restrict__ jobs, int njobs,
                                                  int total_tiles, int nv,
                                                  unsigned long long *__restrict__ status,
-                                                 int only_flagged) {
+                                                 int only_flagged, const int *__restrict__ tile_list,
+                                                 const int *__restrict__ tile_count) {
   using T = typename std::conditional<R32, float, double>::type;
   constexpr int TRI = tri_size<M>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -123,7 +126,11 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
 #define TRI_(r, c) tri[(size_t)tri_at((r), (c)) * TPB + tid]
 #define GEO_(k, q) geo[(size_t)((k) * GEO + (q)) * TPB + tid]
 
-  for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+  // the FP64 re-solve walks the list of tiles the FP32R pass recorded; the other passes walk
+  // every tile
+  const int ntodo = tile_list ? *tile_count : total_tiles;
+  for (int kt = blockIdx.x; kt < ntodo; kt += gridDim.x) {
+    const int tile = tile_list ? tile_list[kt] : kt;
     const int jid = find_job(jobs, njobs, tile);
     const BFJob job = jobs[jid];
     const BFData d = datas[job.data];
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
     if constexpr (R32) {
       if (!ok && active) {
         // float pivot failed: leave this location to the FP64 kernel
-        job.flags[i] = 1;
+        nngp_flag_for_fp64(job, i);
         active = false;
         mi = 0;
       }
@@ -351,7 +358,7 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
       // a conditional variance this small is dominated by the float rounding of C:
       // hand the location to the FP64 kernel
       if (active && !(Fi > kFp32rMinF * (sigmaSq + tauSq))) {
-        job.flags[i] = 1;
+        nngp_flag_for_fp64(job, i);
         active = false;
         mi = 0;
       }
@@ -440,8 +447,17 @@ int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass) {
   const int tiles = fallback_pass ? pl->tiles_fb : pl->tiles;
   const BFJob *jobs = fallback_pass ? pl->d_jobs_fb : pl->d_jobs;
   if (tiles <= 0) return NNGP_OK;
-  kern<<<tiles, TPB, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, jobs, pl->njobs, tiles, pl->nv,
-                                          pl->d_status, fallback_pass ? 1 : 0);
+  // the re-solve pass: a grid of about two blocks per SM walks the recorded tiles (none
+  // recorded: every block returns at once)
+  int grid = tiles;
+  if (fallback_pass) {
+    const int cap = 2 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
+    grid = tiles < cap ? tiles : cap;
+  }
+  kern<<<grid, TPB, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, jobs, pl->njobs, tiles, pl->nv,
+                                         pl->d_status, fallback_pass ? 1 : 0,
+                                         fallback_pass ? pl->d_fb_list : nullptr,
+                                         fallback_pass ? (const int *)pl->d_fb_words : nullptr);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -25,10 +26,21 @@ enum ScratchSlot {
   S_COORDS = 0, S_NNINDX, S_NNLU, S_B, S_F, S_V, S_PARTIAL, S_RED, S_THETA, S_STATUS,
   S_U, S_V2, S_IDX, S_IDX2, S_SORT_TMP, S_XS, S_YS, S_OS, S_NNDIST, S_COORDS0,
   S_NNINDX0, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4, S_OUT5, S_STREAM_N, S_STREAM_U,
-  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_XYF, S_NUM_SLOTS
+  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_XYF, S_VF, S_NUM_SLOTS
 };
 
 struct BFPlan;
+
+// Launch shape of the register B/F kernel chosen by the autotuner for one kernel variant
+// and size class: warps per block, and the grid (0: one block per wpb warp tiles; k > 0: a
+// persistent grid of k x occupancy x SMs blocks).  `ms` is the timed pass, `detail` lists
+// every candidate's time.
+struct TuneEntry {
+  int wpb = 4;
+  int grid_mode = 0;
+  double ms = 0.0;
+  std::string detail;
+};
 
 struct nngp_ctx {
   int device = 0;
@@ -50,6 +62,11 @@ struct nngp_ctx {
   // last single-evaluation plan, reused while its key (pointers, sizes, mode) is unchanged
   BFPlan *cache_plan = nullptr;
   std::string cache_key;
+  // register B/F kernel launch shapes: autotuned on first use (outside stream capture), or
+  // forced by nngp_set_launch_shape (force_wpb > 0)
+  bool autotune = true;
+  int force_wpb = 0, force_grid_mode = 0;
+  std::map<std::string, TuneEntry> tuned;
 };
 void nngp_bf_cache_release(nngp_ctx *ctx);
 
@@ -131,6 +148,8 @@ struct BFData {
   const int *nnIndx;     // packed neighbor lists
   const int *nnLU;       // [offsets | counts], 2n
   const double *V;       // n x nv row-major, fused pass only
+  const float2 *Vf;      // V as float (hi, lo) pairs, n x nv row-major: the FP32R fused pass
+                         // (filled by the plan when the caller leaves it null)
   double *B;             // nIndx, standalone pass only
   double *F;             // n, standalone pass only
 };
@@ -142,7 +161,24 @@ struct BFJob {
   int ntiles;
   double *partial;       // ntiles x NG per-tile partial sums
   unsigned char *flags;  // n bytes: locations the FP32R kernel hands to the FP64 kernel
+  // FP32R primary jobs: where a flagged location's FP64 re-solve tile is recorded (the plan's
+  // [count | marks] words and tile list); fb_tile0 / fb_tpb place location i in FP64 tile
+  // fb_tile0 + i / fb_tpb
+  int fb_tile0;
+  int fb_tpb;
+  unsigned *fb_marks;
+  int *fb_count;
+  int *fb_list;
 };
+
+// Records that FP32R location i of `job` goes to the FP64 kernel: its flag, and its FP64 tile
+// once in the tile list (the list's order varies from run to run; each listed tile writes its
+// own partial slot, so the sums do not).
+__device__ __forceinline__ void nngp_flag_for_fp64(const BFJob &job, int i) {
+  job.flags[i] = 1;
+  const int ft = job.fb_tile0 + i / job.fb_tpb;
+  if (atomicExch(job.fb_marks + ft, 1u) == 0u) job.fb_list[atomicAdd(job.fb_count, 1)] = ft;
+}
 
 // A prepared B/F pass over a set of (dataset, parameter set) evaluations.  The
 // job tables live on the device, so nngp_bf_run only launches kernels (it can be
@@ -150,6 +186,7 @@ struct BFJob {
 // run time, so callers may rewrite them between runs.
 struct BFPlan {
   int precision = 0, mode = 0, mmax = 0, nv = 0, ng = 0;
+  int reg_m = 0;  // > 0: the primary pass runs the register kernel instantiated for this M
   int cov = 4;  // NNGP_COV_* code of the kernels the plan runs (NNGP_COV_ANY: any parameter set)
   int njobs = 0, tiles = 0, tiles_fb = 0;
   BFData *d_datas = nullptr;
@@ -158,6 +195,9 @@ struct BFPlan {
   double *d_partial = nullptr, *d_partial_fb = nullptr;
   unsigned char *d_flags = nullptr;
   size_t flags_bytes = 0;
+  // FP32R: [count | marks (tiles_fb)] words and the list of FP64 tiles to re-solve
+  unsigned *d_fb_words = nullptr;
+  int *d_fb_list = nullptr;
   unsigned long long *d_status = nullptr;
   std::vector<void *> owned;
 };
@@ -195,6 +235,32 @@ void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *plan);
 // Stream-ordered device allocation (pooled), freed with nngp_free_async.
 void *nngp_malloc_async(nngp_ctx *ctx, size_t bytes);
 void nngp_free_async(nngp_ctx *ctx, void *p);
+
+// Neighbor bounds the register FP32R kernel is instantiated for (m <= 16), ascending.
+constexpr int NNGP_REG_MS[] = {10, 15, 16};
+// The smallest instantiated bound >= m, or 0 when the register kernel does not apply.
+inline int nngp_reg_m(int precision, int mmax) {
+  if (precision != NNGP_FP32R) return 0;
+  for (int M : NNGP_REG_MS)
+    if (mmax <= M) return M;
+  return 0;
+}
+// Shared memory of the register kernel: per lane the double-float covariance (hi and lo
+// parts of the strict lower triangle and the c vector) and one float4 of geometry per
+// neighbor (the epilogue's staging of 2 NNGP_MAX_NV + 2 (1 + NV(NV+1)/2) floats reuses it);
+// per warp a 64-float exp table.  Blocks hold at most 8 warps and 227 KB.
+constexpr int nngp_bfr_lane_floats(int M) {
+  const int raw = 2 * (M * (M - 1) / 2 + M) + 4 * M;
+  const int red = 2 * NNGP_MAX_NV + 2 * (1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2);
+  return ((raw > red ? raw : red) + 3) & ~3;
+}
+constexpr size_t nngp_bfr_warp_bytes(int M) { return sizeof(float) * (32 * (size_t)nngp_bfr_lane_floats(M) + 64); }
+constexpr int nngp_bfr_max_wpb(int M) {
+  const int w = (int)((size_t)227 * 1024 / nngp_bfr_warp_bytes(M));
+  return w < 8 ? w : 8;
+}
+// Writes V (n x nv row-major doubles) as float (hi, lo) pairs.
+int nngp_split_v(nngp_ctx *ctx, const double *V, int64_t count, float2 *Vf);
 
 // Writes the interleaved double coordinates (xy, may be null) and their float hi/lo
 // split (xyf, may be null) from the n x 2 column-major coordinates.

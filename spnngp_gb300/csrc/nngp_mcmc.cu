@@ -354,10 +354,17 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     cov_prepare(cp);
     th[2 * k] = th[2 * k + 1] = cp;
   }
-  // Instances are split into classes by neighbor count (m <= 16 or <= 32) and by correlation
-  // code -- the model, with Matern needing the general-nu kernel when nu is sampled or starts
-  // off the half-integers -- so each class runs the kernel instantiation it needs and no other.
-  constexpr int NCLS = 10;
+  // Instances are split into classes by neighbor bound and by correlation code -- the model,
+  // with Matern needing the general-nu kernel when nu is sampled or starts off the
+  // half-integers -- so each class runs the kernel instantiation it needs and no other.  The
+  // bounds are those the kernels are built for: FP32R 10 / 15 / 16 (register kernel) and 32;
+  // FP64 16 and 32.
+  constexpr int NCLS = 20;
+  auto bound_class = [&](int m) {
+    if (m > 16) return 3;
+    if (precision != NNGP_FP32R) return 2;
+    return m <= 10 ? 0 : (m <= 15 ? 1 : 2);
+  };
   std::vector<int> cls(ninst), pos(ninst);
   std::vector<std::vector<BFData>> cdatas(NCLS);
   std::vector<std::vector<PassEval>> cevCand(NCLS), cevCur(NCLS);
@@ -365,7 +372,7 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     const MCInstance &I = insts[k];
     const bool gen = I.model == 2 && (I.tuning[3] != 0.0 || th[2 * k].halfk < 0);
     const int cov = gen ? NNGP_COV_ANY : I.model;
-    cls[k] = (I.m <= 16 ? 0 : 5) + cov;
+    cls[k] = 5 * bound_class(I.m) + cov;
     pos[k] = (int)cdatas[cls[k]].size();
     cdatas[cls[k]].push_back(datas[k]);
     cevCand[cls[k]].push_back(PassEval{pos[k], 2 * k + 1});

@@ -1,0 +1,122 @@
+"""The FP32R register kernel (neighbor counts m <= 16): B, F and the fused likelihood sums
+against the FP64 form and the oracle, for every correlation model and every compiled
+neighbor bound; results independent of the launch shape the autotuner picks."""
+import numpy as np
+import pytest
+
+from conftest import cm, xorder
+
+pytestmark = pytest.mark.gpu
+
+# FP32R against FP64 (the stated bounds): log-likelihood, per-location F (relative) and B
+# (relative to the largest |B|).  The refinement residual uses the covariance in
+# double-float, and a location whose estimated F error exceeds 1e-8 F is re-solved in FP64.
+TOL_LOGLIK = 1e-6
+TOL_F = 1e-6
+TOL_B = 1e-6
+
+MODELS = [("exponential", (1.0, 0.1, 6.0)), ("exponential", (1.0, 0.0, 59.91)),
+          ("spherical", (2.0, 0.2, 3.0)), ("matern", (1.0, 0.1, 9.488, 1.5)),
+          ("matern", (1.0, 0.1, 30.0, 2.5)), ("matern", (1.0, 0.2, 12.0, 0.8)),
+          ("gaussian", (1.0, 1e-6, 34.62)), ("gaussian", (1.0, 1e-6, 3.462)), ("gaussian", (1.0, 0.05, 4.0))]
+
+
+def dataset(n, seed, nv=3):
+    rng = np.random.default_rng(seed)
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n)] + [rng.normal(size=n) for _ in range(nv - 2)])
+    y = X @ np.linspace(1.0, -0.5, nv - 1) + rng.normal(size=n)
+    return c, X, y
+
+
+def loglik(ld, G, beta):
+    p = len(beta)
+    return -0.5 * (ld + beta @ G[:p, :p] @ beta - 2 * beta @ G[:p, p] + G[p, p])
+
+
+@pytest.mark.parametrize("model,theta", MODELS)
+@pytest.mark.parametrize("m", [5, 10, 12, 15, 16])
+def test_fp32r_B_F_against_fp64(sp, orc, model, theta, m):
+    c, X, y = dataset(3000, 10 + m)
+    o = orc.mkNNIndxCB(cm(c), m)
+    B64, F64, ld64 = sp.updateBF(c, o[0], o[2], m, model, theta, "fp64")
+    B32, F32, ld32 = sp.updateBF(c, o[0], o[2], m, model, theta, "fp32r")
+    assert np.all(np.isfinite(B32)) and np.all(F32 > 0)
+    assert np.max(np.abs(F32 - F64) / F64) <= TOL_F
+    assert abs(ld32 - ld64) <= TOL_LOGLIK * max(1.0, abs(ld64))
+    assert np.max(np.abs(B32 - B64)) <= TOL_B * max(1.0, np.max(np.abs(B64)))
+
+
+@pytest.mark.parametrize("model,theta", MODELS)
+@pytest.mark.parametrize("m,nv", [(10, 2), (15, 3), (16, 5)])
+def test_fp32r_fused_loglik_against_fp64(sp, orc, model, theta, m, nv):
+    c, X, y = dataset(5000, 20 + m, nv)
+    o = orc.mkNNIndxCB(cm(c), m)
+    V = np.column_stack([X, y])
+    ld64, G64 = sp.loglik_gram(c, o[0], o[2], m, V, model, theta, "fp64")
+    ld32, G32 = sp.loglik_gram(c, o[0], o[2], m, V, model, theta, "fp32r")
+    beta = np.linspace(1.0, -0.5, nv - 1)
+    ll64, ll32 = loglik(ld64, G64, beta), loglik(ld32, G32, beta)
+    assert abs(ll32 - ll64) <= TOL_LOGLIK * abs(ll64)
+    assert np.max(np.abs(G32 - G64)) <= 1e-6 * np.max(np.abs(G64))
+
+
+def test_fp32r_matches_oracle_loglik(sp, orc):
+    """The fused FP32R pass against the oracle's port of updateBF + Q (src/rNNGP.cpp:306-317)."""
+    c, X, y = dataset(4000, 33)
+    m = 15
+    o = orc.mkNNIndxCB(cm(c), m)
+    theta = (1.3, 0.2, 11.0)
+    Bo, Fo, ldo, st = orc.updateBF(cm(c), o[0], o[2], m, 0, *theta, 0.0)
+    assert st == 0
+    beta = np.array([1.0, 0.25])
+    r = X @ beta - y
+    llo = -0.5 * (ldo + orc.Q(Bo, Fo, r, r, o[0], o[2]))
+    ld, G = sp.loglik_gram(c, o[0], o[2], m, np.column_stack([X, y]), "exponential", theta, "fp32r")
+    assert abs(loglik(ld, G, beta) - llo) <= TOL_LOGLIK * abs(llo)
+
+
+SHAPES = [(1, 0), (2, 0), (4, 0), (8, 0), (1, 1), (4, 1), (8, 2), (2, 2)]
+
+
+@pytest.mark.parametrize("m", [10, 15, 16])
+def test_launch_shape_does_not_change_results(sp, orc, m):
+    """Every launch shape the autotuner may pick gives bitwise-identical results."""
+    c, X, y = dataset(7001, 40 + m)
+    o = orc.mkNNIndxCB(cm(c), m)
+    V = np.column_stack([X, y])
+    ctx = sp.default_context()
+    ref = None
+    try:
+        for wpb, gm in SHAPES:
+            ctx.set_launch_shape(wpb, gm)
+            B, F, ld = sp.updateBF(c, o[0], o[2], m, "exponential", (1.0, 0.1, 8.0), "fp32r")
+            ldg, G = sp.loglik_gram(c, o[0], o[2], m, V, "exponential", (1.0, 0.1, 8.0), "fp32r")
+            got = (B, F, np.array([ld]), np.array([ldg]), G)
+            if ref is None:
+                ref = got
+            else:
+                for a, b in zip(ref, got):
+                    assert np.array_equal(a, b), (wpb, gm)
+    finally:
+        ctx.set_launch_shape(0, 0)
+    ldt, Gt = sp.loglik_gram(c, o[0], o[2], m, V, "exponential", (1.0, 0.1, 8.0), "fp32r")
+    assert ldt == ref[3][0] and np.array_equal(Gt, ref[4])
+
+
+def test_autotune_reports_choice(sp, orc):
+    ctx = sp.Context(0)
+    c, X, y = dataset(20000, 77)
+    o = orc.mkNNIndxCB(cm(c), 15)
+    V = np.column_stack([X, y])
+    sp.loglik_gram(c, o[0], o[2], 15, V, "gaussian", (1.0, 0.1, 5.0), "fp32r", ctx=ctx)
+    rep = ctx.autotune_report()
+    key = [k for k in rep if k.startswith("M=15 mode=1 cov=3")]
+    assert len(key) == 1
+    e = rep[key[0]]
+    assert 1 <= e["wpb"] <= 8 and len(e["candidates"]) >= 4
+    assert e["ms"] == pytest.approx(min(e["candidates"].values()), rel=1e-3, abs=1e-4)
+    # a second pass of the same class reuses the choice
+    sp.loglik_gram(c, o[0], o[2], 15, V, "gaussian", (1.0, 0.1, 5.0), "fp32r", ctx=ctx)
+    assert ctx.autotune_report() == rep
+    ctx.close()
