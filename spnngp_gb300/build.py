@@ -28,10 +28,10 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 
 # source -> [(object suffix, defines)]: sources compiled once per variant
 # (FP32R with m <= 16 runs the register kernel of nngp_bfr_inst.cu, so the shared-memory
-# kernel is built in FP32R for the 32-neighbor bound only)
+# kernel is built in FP32R for the 24- and 32-neighbor bounds only)
 VARIANTS = {
     "nngp_bf_inst.cu": [(f"_m{m}_{'f' if r else 'd'}_c{c}", [f"-DBF_M={m}", f"-DBF_R32={r}", f"-DBF_COV={c}"])
-                        for m, r in ((16, 0), (32, 1), (32, 0)) for c in (0, 1, 2, 3, 4)],
+                        for m, r in ((16, 0), (24, 1), (24, 0), (32, 1), (32, 0)) for c in (0, 1, 2, 3, 4)],
     "nngp_bfr_inst.cu": [(f"_m{m}_c{c}", [f"-DBFR_M={m}", f"-DBFR_COV={c}"])
                          for m in (10, 15, 16) for c in (0, 1, 2, 3, 4)],
 }
@@ -91,7 +91,8 @@ def build(verbose: bool = False, extra: list[str] | None = None, force: bool = F
                 if rc != 0:
                     raise RuntimeError(f"nvcc failed on {os.path.basename(src)}")
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs]
+        # --no-undefined: a symbol missing from every object fails the link, not the first dlopen
+        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-Xlinker", "--no-undefined", "-o", LIB, *objs]
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:
             sys.stderr.write(p.stdout + p.stderr)

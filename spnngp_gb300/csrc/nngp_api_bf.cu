@@ -7,11 +7,12 @@
 
 namespace {
 
-// col-major n x nv -> row-major n x nv, and (when rmf is given) its float (hi, lo) split
-__global__ void to_row_major_kernel(const double *__restrict__ cm, int n, int nv, double *__restrict__ rm,
-                                    float2 *__restrict__ rmf) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < (long)n * nv) {
+// col-major n x nv -> row-major n x nv, and (when rmf is given) its float (hi, lo) split, for
+// locations [i0, i1)
+__global__ void to_row_major_kernel(const double *__restrict__ cm, int n, int nv, int i0, int i1,
+                                    double *__restrict__ rm, float2 *__restrict__ rmf) {
+  const long t = (long)i0 * nv + (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long)i1 * nv) {
     const int i = (int)(t / nv), v = (int)(t % nv);
     const double x = cm[(size_t)v * n + i];
     rm[t] = x;
@@ -84,10 +85,35 @@ CovParams make_params(int covModel, double sigmaSq, double tauSq, double phi, do
   return c;
 }
 
-// Single-evaluation pass on resident data.  coords are n x 2 column-major (device).
+// Host arrays a host-pointer entry point streams in (each null when already on the device).
+struct HostIn {
+  const double *coords = nullptr;  // n x 2 column-major
+  const int *nnIndx = nullptr;
+  const int *nnLU = nullptr;       // [offsets | counts]
+  const double *V = nullptr;       // n x nv column-major
+};
+
+// Location chunks of the streamed form: about 128 K locations each (at most 8), boundaries on
+// multiples of 128 so they fall on tile boundaries of every kernel.
+std::vector<int> chunk_bounds(int n) {
+  int k = n / 131072;
+  k = k < 1 ? 1 : (k > 8 ? 8 : k);
+  std::vector<int> b{0};
+  const int step = ((n + k - 1) / k + 127) & ~127;
+  for (int a = step; a < n; a += step) b.push_back(a);
+  b.push_back(n);
+  return b;
+}
+
+// Single-evaluation pass.  coords are n x 2 column-major (device).  With `hin`, the device
+// arrays d_coords_cm, d_nnIndx, d_nnLU and d_V_cm are filled from host memory here, one
+// location chunk at a time on the copy stream, and each chunk's conversions and B/F tiles run
+// as soon as its copies land (the neighbors of a location precede it in the ordering, so they
+// are in the same or an earlier chunk).  The pass is the same either way: one job over all
+// locations whose tiles are launched in pieces, so results do not depend on the chunking.
 int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_coords_cm,
                const int *d_nnIndx, const int *d_nnLU, const double *d_V_cm, const CovParams &cp,
-               int precision, double *d_B, double *d_F, double *h_out) {
+               int precision, double *d_B, double *d_F, double *h_out, const HostIn *hin = nullptr) {
   if (precision != NNGP_FP64 && precision != NNGP_FP32R)
     return nngp_fail(ctx, NNGP_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32R)");
   double *xy, *Vrm = nullptr;
@@ -95,16 +121,11 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   float2 *Vf = nullptr;
   NNGP_ALLOC(ctx, xy, double, S_COORDS, 2 * (size_t)n);
   if (precision == NNGP_FP32R) NNGP_ALLOC(ctx, xyf, float, S_XYF, 4 * (size_t)n);
-  int st0 = nngp_prepare_coords(ctx, d_coords_cm, n, xy, xyf);
-  if (st0) return st0;
   if (mode == 1) {
     NNGP_ALLOC(ctx, Vrm, double, S_V, (size_t)n * nv);
     // V changes from call to call under a cached plan: the register kernel's float split is
     // refreshed here rather than by the plan
     if (nngp_reg_m(precision, m) > 0) NNGP_ALLOC(ctx, Vf, float2, S_VF, (size_t)n * nv);
-    const long tot = (long)n * nv;
-    to_row_major_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(d_V_cm, n, nv, Vrm, Vf);
-    NNGP_LAUNCH_CHECK(ctx);
   }
   CovParams *d_theta;
   unsigned long long *d_status;
@@ -113,9 +134,6 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   NNGP_ALLOC(ctx, d_status, unsigned long long, S_STATUS, 1);
   const int ng = mode == 1 ? 1 + nv * (nv + 1) / 2 : 1;
   NNGP_ALLOC(ctx, d_out, double, S_RED, 2 * (size_t)ng);
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(d_theta, &cp, sizeof cp, cudaMemcpyHostToDevice, ctx->stream));
-  int st = nngp_reset_status(ctx, d_status);
-  if (st) return st;
   BFData d{};
   d.n = n;
   d.m = m;
@@ -133,6 +151,7 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
            (const void *)xyf, (const void *)Vf,
            (const void *)d_nnIndx, (const void *)d_nnLU, (const void *)Vrm, (void *)d_B, (void *)d_F,
            (void *)d_theta, (void *)d_status);
+  int st = NNGP_OK;
   if (!ctx->cache_plan || ctx->cache_key != key) {
     nngp_bf_cache_release(ctx);
     BFPlan *plan = new BFPlan();
@@ -146,9 +165,57 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
     ctx->cache_plan = plan;
     ctx->cache_key = key;
   }
-  st = nngp_bf_run(ctx, ctx->cache_plan, d_out);
-  if (!st) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, d_out, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx->stream));
-  if (st) return st;
+  const BFPlan *pl = ctx->cache_plan;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(d_theta, &cp, sizeof cp, cudaMemcpyHostToDevice, ctx->stream));
+  if ((st = nngp_reset_status(ctx, d_status))) return st;
+  if ((st = nngp_bf_begin(ctx, pl))) return st;
+  const int tile = nngp_bf_tile(precision, m);
+  const std::vector<int> bounds = hin ? chunk_bounds(n) : std::vector<int>{0, n};
+  const int nchunks = (int)bounds.size() - 1;
+  cudaStream_t cs = ctx->stream;
+  if (hin) {
+    if (!ctx->copy_stream) NNGP_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    cs = ctx->copy_stream;
+    while ((int)ctx->chunk_events.size() < nchunks + 1) {
+      cudaEvent_t e;
+      NNGP_CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ctx->chunk_events.push_back(e);
+    }
+    // the copies overwrite buffers the previous call's kernels read: start after them
+    NNGP_CUDA_TRY(ctx, cudaEventRecord(ctx->chunk_events[nchunks], ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaStreamWaitEvent(cs, ctx->chunk_events[nchunks], 0));
+  }
+  for (int k = 0; k < nchunks; k++) {
+    const int a = bounds[k], b = bounds[k + 1];
+    if (hin) {
+      auto h2d = [&](void *dst, const void *src, size_t bytes) {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, cs) : cudaSuccess;
+      };
+      double *dc = const_cast<double *>(d_coords_cm);
+      int *dlu = const_cast<int *>(d_nnLU), *dnn = const_cast<int *>(d_nnIndx);
+      const int64_t o0 = hin->nnLU[a], o1 = (int64_t)hin->nnLU[b - 1] + hin->nnLU[n + b - 1];
+      NNGP_CUDA_TRY(ctx, h2d(dc + a, hin->coords + a, sizeof(double) * (b - a)));
+      NNGP_CUDA_TRY(ctx, h2d(dc + n + a, hin->coords + n + a, sizeof(double) * (b - a)));
+      NNGP_CUDA_TRY(ctx, h2d(dlu + a, hin->nnLU + a, sizeof(int) * (b - a)));
+      NNGP_CUDA_TRY(ctx, h2d(dlu + n + a, hin->nnLU + n + a, sizeof(int) * (b - a)));
+      NNGP_CUDA_TRY(ctx, h2d(dnn + o0, hin->nnIndx + o0, sizeof(int) * (size_t)(o1 - o0)));
+      if (mode == 1)
+        for (int v = 0; v < nv; v++)
+          NNGP_CUDA_TRY(ctx, h2d(const_cast<double *>(d_V_cm) + (size_t)v * n + a, hin->V + (size_t)v * n + a,
+                                 sizeof(double) * (b - a)));
+      NNGP_CUDA_TRY(ctx, cudaEventRecord(ctx->chunk_events[k], cs));
+      NNGP_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_events[k], 0));
+    }
+    if ((st = nngp_prepare_coords(ctx, d_coords_cm, n, xy, xyf, a, b))) return st;
+    if (mode == 1) {
+      const long cnt = (long)(b - a) * nv;
+      to_row_major_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, ctx->stream>>>(d_V_cm, n, nv, a, b, Vrm, Vf);
+      NNGP_LAUNCH_CHECK(ctx);
+    }
+    if ((st = nngp_bf_primary(ctx, pl, a / tile, (b + tile - 1) / tile))) return st;
+  }
+  if ((st = nngp_bf_finish(ctx, pl, d_out))) return st;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, d_out, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx->stream));
   return nngp_check_status(ctx, d_status, mode == 0 ? "updateBF" : "loglik_gram");
 }
 
@@ -161,24 +228,6 @@ void unpack_gram(const double *packed, int nv, double *gram) {
       gram[(size_t)a * nv + b] = packed[k];
       k++;
     }
-}
-
-struct HostUpload {
-  double *coords = nullptr;
-  int *nnIndx = nullptr, *nnLU = nullptr;
-};
-
-int upload_graph(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
-                 const int *nnIndxLU, HostUpload &u) {
-  const int64_t nI = nngp_nindx(n, m);
-  NNGP_ALLOC(ctx, u.coords, double, S_COORDS0, 2 * (size_t)n);
-  NNGP_ALLOC(ctx, u.nnIndx, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
-  NNGP_ALLOC(ctx, u.nnLU, int, S_NNLU, 2 * (size_t)n);
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u.coords, coords, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
-  if (nI > 0)
-    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u.nnIndx, nnIndx, sizeof(int) * nI, cudaMemcpyHostToDevice, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(u.nnLU, nnIndxLU, sizeof(int) * 2 * n, cudaMemcpyHostToDevice, ctx->stream));
-  return NNGP_OK;
 }
 
 }  // namespace
@@ -225,14 +274,20 @@ int nngp_updateBF(nngp_ctx *ctx, int n, int m, const double *coords, const int *
   int st = check_common(ctx, n, m, covModel);
   if (st) return st;
   cudaSetDevice(ctx->device);
-  HostUpload u;
-  if ((st = upload_graph(ctx, n, m, coords, nnIndx, nnIndxLU, u))) return st;
   const int64_t nI = nngp_nindx(n, m);
-  double *dB, *dF;
+  double *dc, *dB, *dF;
+  int *dnn, *dlu;
+  NNGP_ALLOC(ctx, dc, double, S_COORDS0, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, dnn, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dlu, int, S_NNLU, 2 * (size_t)n);
   NNGP_ALLOC(ctx, dB, double, S_B, (size_t)(nI > 0 ? nI : 1));
   NNGP_ALLOC(ctx, dF, double, S_F, (size_t)n);
   const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
-  st = run_single(ctx, 0, n, m, 0, u.coords, u.nnIndx, u.nnLU, nullptr, cp, precision, dB, dF, logDet);
+  HostIn hin;
+  hin.coords = coords;
+  hin.nnIndx = nnIndx;
+  hin.nnLU = nnIndxLU;
+  st = run_single(ctx, 0, n, m, 0, dc, dnn, dlu, nullptr, cp, precision, dB, dF, logDet, &hin);
   if (st) return st;
   if (nI > 0) NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(B, dB, sizeof(double) * nI, cudaMemcpyDeviceToHost, ctx->stream));
   NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(F, dF, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
@@ -257,14 +312,21 @@ int nngp_loglik_gram(nngp_ctx *ctx, int n, int m, int nv, const double *coords,
   if (st) return st;
   if (nv < 1 || nv > NNGP_MAX_NV) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= nv <= 8 required");
   cudaSetDevice(ctx->device);
-  HostUpload u;
-  if ((st = upload_graph(ctx, n, m, coords, nnIndx, nnIndxLU, u))) return st;
-  double *dV;
+  const int64_t nI = nngp_nindx(n, m);
+  double *dc, *dV;
+  int *dnn, *dlu;
+  NNGP_ALLOC(ctx, dc, double, S_COORDS0, 2 * (size_t)n);
+  NNGP_ALLOC(ctx, dnn, int, S_NNINDX, (size_t)(nI > 0 ? nI : 1));
+  NNGP_ALLOC(ctx, dlu, int, S_NNLU, 2 * (size_t)n);
   NNGP_ALLOC(ctx, dV, double, S_V2, (size_t)n * nv);
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(dV, V, sizeof(double) * n * nv, cudaMemcpyHostToDevice, ctx->stream));
   const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
+  HostIn hin;
+  hin.coords = coords;
+  hin.nnIndx = nnIndx;
+  hin.nnLU = nnIndxLU;
+  hin.V = V;
   double packed[1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2];
-  st = run_single(ctx, 1, n, m, nv, u.coords, u.nnIndx, u.nnLU, dV, cp, precision, nullptr, nullptr, packed);
+  st = run_single(ctx, 1, n, m, nv, dc, dnn, dlu, dV, cp, precision, nullptr, nullptr, packed, &hin);
   if (st) return st;
   *logDet = packed[0];
   unpack_gram(packed + 1, nv, gram);

@@ -12,7 +12,7 @@
 // nngp_bf_kernel.cuh and nngp_bfr_kernel.cuh.
 namespace nngp_bf {
 template <int M, bool R32, int MODE, int COV>
-int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass);
+int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
 template <int M, bool R32>
 constexpr int bf_tpb() {
   return R32 ? (M <= 16 ? 128 : 64) : (M <= 16 ? 64 : 32);
@@ -20,7 +20,7 @@ constexpr int bf_tpb() {
 }  // namespace nngp_bf
 namespace nngp_bfr {
 template <int M, int MODE, int COV>
-int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid);
+int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1);
 template <int M, int MODE, int COV>
 int occupancy(int wpb);
 }  // namespace nngp_bfr
@@ -66,66 +66,77 @@ __global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, const BFJ
 
 namespace {
 template <int MODE, int COV>
-int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
+int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
   // FP32R with m <= 16 runs the register kernel (launched by run_reg); the FP64
   // re-solve of its flagged locations lands here with fp32r false
-  if (pl->mmax <= 16) return launch_one<16, false, MODE, COV>(ctx, pl, fallback_pass);
-  return fp32r ? launch_one<32, true, MODE, COV>(ctx, pl, fallback_pass)
-               : launch_one<32, false, MODE, COV>(ctx, pl, fallback_pass);
+  if (pl->mmax <= 16) return launch_one<16, false, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  if (pl->mmax <= 24)
+    return fp32r ? launch_one<24, true, MODE, COV>(ctx, pl, fallback_pass, t0, t1)
+                 : launch_one<24, false, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  return fp32r ? launch_one<32, true, MODE, COV>(ctx, pl, fallback_pass, t0, t1)
+               : launch_one<32, false, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
 }
 
 template <int MODE>
-int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
+int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
   switch (pl->cov) {
-    case NNGP_COV_EXP: return launch_mode_c<MODE, NNGP_COV_EXP>(ctx, pl, fp32r, fallback_pass);
-    case NNGP_COV_SPH: return launch_mode_c<MODE, NNGP_COV_SPH>(ctx, pl, fp32r, fallback_pass);
-    case NNGP_COV_MAT_HALF: return launch_mode_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, fp32r, fallback_pass);
-    case NNGP_COV_GAU: return launch_mode_c<MODE, NNGP_COV_GAU>(ctx, pl, fp32r, fallback_pass);
-    default: return launch_mode_c<MODE, NNGP_COV_ANY>(ctx, pl, fp32r, fallback_pass);
+    case NNGP_COV_EXP: return launch_mode_c<MODE, NNGP_COV_EXP>(ctx, pl, fp32r, fallback_pass, t0, t1);
+    case NNGP_COV_SPH: return launch_mode_c<MODE, NNGP_COV_SPH>(ctx, pl, fp32r, fallback_pass, t0, t1);
+    case NNGP_COV_MAT_HALF: return launch_mode_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, fp32r, fallback_pass, t0, t1);
+    case NNGP_COV_GAU: return launch_mode_c<MODE, NNGP_COV_GAU>(ctx, pl, fp32r, fallback_pass, t0, t1);
+    default: return launch_mode_c<MODE, NNGP_COV_ANY>(ctx, pl, fp32r, fallback_pass, t0, t1);
   }
 }
 
 // ---------------------------------------------------------------- register kernel
 // Calls launch_reg (query_occ false) or occupancy (true) of the plan's instantiation.
 template <int M, int MODE>
-int reg_call_m(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ) {
+int reg_call_m(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ, int t0, int t1) {
   using namespace nngp_bfr;
   switch (pl->cov) {
     case NNGP_COV_EXP:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_EXP>(wpb) : launch_reg<M, MODE, NNGP_COV_EXP>(ctx, pl, wpb, grid);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_EXP>(wpb) : launch_reg<M, MODE, NNGP_COV_EXP>(ctx, pl, wpb, grid, t0, t1);
     case NNGP_COV_SPH:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_SPH>(wpb) : launch_reg<M, MODE, NNGP_COV_SPH>(ctx, pl, wpb, grid);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_SPH>(wpb) : launch_reg<M, MODE, NNGP_COV_SPH>(ctx, pl, wpb, grid, t0, t1);
     case NNGP_COV_MAT_HALF:
       return query_occ ? occupancy<M, MODE, NNGP_COV_MAT_HALF>(wpb)
-                       : launch_reg<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, wpb, grid);
+                       : launch_reg<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, wpb, grid, t0, t1);
     case NNGP_COV_GAU:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_GAU>(wpb) : launch_reg<M, MODE, NNGP_COV_GAU>(ctx, pl, wpb, grid);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_GAU>(wpb) : launch_reg<M, MODE, NNGP_COV_GAU>(ctx, pl, wpb, grid, t0, t1);
     default:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_ANY>(wpb) : launch_reg<M, MODE, NNGP_COV_ANY>(ctx, pl, wpb, grid);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_ANY>(wpb) : launch_reg<M, MODE, NNGP_COV_ANY>(ctx, pl, wpb, grid, t0, t1);
   }
 }
-int reg_call(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ) {
+int reg_call(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ, int t0 = 0, int t1 = 0) {
   const bool m1 = pl->mode == 1;
   switch (pl->reg_m) {
-    case 10: return m1 ? reg_call_m<10, 1>(ctx, pl, wpb, grid, query_occ) : reg_call_m<10, 0>(ctx, pl, wpb, grid, query_occ);
-    case 15: return m1 ? reg_call_m<15, 1>(ctx, pl, wpb, grid, query_occ) : reg_call_m<15, 0>(ctx, pl, wpb, grid, query_occ);
-    default: return m1 ? reg_call_m<16, 1>(ctx, pl, wpb, grid, query_occ) : reg_call_m<16, 0>(ctx, pl, wpb, grid, query_occ);
+    case 10:
+      return m1 ? reg_call_m<10, 1>(ctx, pl, wpb, grid, query_occ, t0, t1)
+                : reg_call_m<10, 0>(ctx, pl, wpb, grid, query_occ, t0, t1);
+    case 15:
+      return m1 ? reg_call_m<15, 1>(ctx, pl, wpb, grid, query_occ, t0, t1)
+                : reg_call_m<15, 0>(ctx, pl, wpb, grid, query_occ, t0, t1);
+    default:
+      return m1 ? reg_call_m<16, 1>(ctx, pl, wpb, grid, query_occ, t0, t1)
+                : reg_call_m<16, 0>(ctx, pl, wpb, grid, query_occ, t0, t1);
   }
 }
 
 // Blocks of the launch shape (wpb, grid_mode) for this plan: grid_mode 0 gives every warp one
 // tile; k > 0 caps the grid at k x (resident blocks per SM) x SMs, each warp looping over tiles.
-int reg_grid(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid_mode) {
-  const int full = (pl->tiles + wpb - 1) / wpb;
+int reg_grid(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid_mode, int ntiles) {
+  const int full = (ntiles + wpb - 1) / wpb;
   if (grid_mode <= 0) return full > 0 ? full : 1;
   const int occ = reg_call(ctx, pl, wpb, 0, true);
   const long cap = (long)grid_mode * occ * (ctx->sm_count > 0 ? ctx->sm_count : 1);
   return (int)(cap < full ? cap : full);
 }
 
-std::string tune_key(const BFPlan *pl) {
+// Tuning class: kernel variant and size class.  Sizes from the sample cap up share one class
+// (the sample, and so the choice, is the same for them).
+std::string tune_key(const BFPlan *pl, int ntiles) {
   int bucket = 0;
-  while ((1 << (bucket + 1)) <= pl->tiles) bucket++;
+  while ((1 << (bucket + 1)) <= ntiles && (1 << (bucket + 1)) <= 65536) bucket++;
   char k[96];
   snprintf(k, sizeof k, "M=%d mode=%d cov=%d tiles~2^%d", pl->reg_m, pl->mode, pl->cov, bucket);
   return k;
@@ -133,7 +144,7 @@ std::string tune_key(const BFPlan *pl) {
 
 // Times every candidate shape on the plan itself (each run rewrites the same outputs with
 // the same values: the results do not depend on the shape) and keeps the fastest.
-int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best) {
+int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best, int t0, int t1) {
   static const int kWpb[] = {1, 2, 3, 4, 5, 6, 8};
   static const int kGrid[] = {0, 1, 2};
   cudaEvent_t e0, e1;
@@ -145,13 +156,13 @@ int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best) {
   int st = NNGP_OK;
   for (int wpb : kWpb) {
     if (wpb > nngp_bfr_max_wpb(pl->reg_m)) continue;
-    const int full = reg_grid(ctx, pl, wpb, 0);
+    const int full = reg_grid(ctx, pl, wpb, 0, t1 - t0);
     for (int gm : kGrid) {
-      const int grid = reg_grid(ctx, pl, wpb, gm);
+      const int grid = reg_grid(ctx, pl, wpb, gm, t1 - t0);
       if (gm > 0 && grid >= full) continue;  // same as the one-tile-per-warp grid
-      if ((st = reg_call(ctx, pl, wpb, grid, false))) break;  // warm-up
+      if ((st = reg_call(ctx, pl, wpb, grid, false, t0, t1))) break;  // warm-up
       cudaEventRecord(e0, ctx->stream);
-      if ((st = reg_call(ctx, pl, wpb, grid, false))) break;
+      if ((st = reg_call(ctx, pl, wpb, grid, false, t0, t1))) break;
       cudaEventRecord(e1, ctx->stream);
       if (cudaEventSynchronize(e1) != cudaSuccess) {
         st = nngp_fail(ctx, NNGP_ERR_CUDA, "autotune: event synchronisation failed");
@@ -176,23 +187,30 @@ int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best) {
   return st;
 }
 
-int run_reg(nngp_ctx *ctx, const BFPlan *pl) {
+// Passes smaller than kTuneMinTiles (64 K locations) run the default shape: their time is
+// launch overhead more than shape.  Tuning times candidates on at most kTuneSampleTiles.
+constexpr int kTuneMinTiles = 2048;
+constexpr int kTuneSampleTiles = 65536;
+
+int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   int wpb = 4, gm = 0;
   if (ctx->force_wpb > 0) {
     wpb = ctx->force_wpb;
     gm = ctx->force_grid_mode;
   } else {
-    const std::string key = tune_key(pl);
+    const std::string key = tune_key(pl, t1 - t0);
     auto it = ctx->tuned.find(key);
     if (it != ctx->tuned.end()) {
       wpb = it->second.wpb;
       gm = it->second.grid_mode;
-    } else if (ctx->autotune) {
+    } else if (ctx->autotune && t1 - t0 >= kTuneMinTiles) {
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
       cudaStreamIsCapturing(ctx->stream, &cs);
       if (cs == cudaStreamCaptureStatusNone) {
+        // candidates are timed on a bounded sample of the plan's tiles (a large plan -- a
+        // 5000-job conjugate sweep -- would otherwise spend seconds per candidate)
         TuneEntry e;
-        const int st = tune_reg(ctx, pl, e);
+        const int st = tune_reg(ctx, pl, e, t0, t1 - t0 > kTuneSampleTiles ? t0 + kTuneSampleTiles : t1);
         if (st) return st;
         ctx->tuned[key] = e;
         wpb = e.wpb;
@@ -202,13 +220,14 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl) {
   }
   const int wmax = nngp_bfr_max_wpb(pl->reg_m);
   if (wpb > wmax) wpb = wmax;  // a forced shape larger than the block limit of this bound
-  return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm), false);
+  return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm, t1 - t0), false, t0, t1);
 }
 
-int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
-  if (fp32r && !fallback_pass && pl->reg_m > 0) return run_reg(ctx, pl);
-  return pl->mode == 0 ? launch_mode<0>(ctx, pl, fp32r, fallback_pass)
-                       : launch_mode<1>(ctx, pl, fp32r, fallback_pass);
+// Primary pass over tiles [t0, t1), or (fallback_pass) the FP64 re-solve of the recorded tiles.
+int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
+  if (fp32r && !fallback_pass && pl->reg_m > 0) return run_reg(ctx, pl, t0, t1);
+  return pl->mode == 0 ? launch_mode<0>(ctx, pl, fp32r, fallback_pass, t0, t1)
+                       : launch_mode<1>(ctx, pl, fp32r, fallback_pass, t0, t1);
 }
 
 }  // namespace
@@ -333,16 +352,21 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
   return NNGP_OK;
 }
 
-int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
-  int st;
-  const bool fp32r = pl->precision == NNGP_FP32R;
-  if (fp32r) {
+int nngp_bf_begin(nngp_ctx *ctx, const BFPlan *pl) {
+  if (pl->precision == NNGP_FP32R) {
     NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_flags, 0, pl->flags_bytes, ctx->stream));
     NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_fb_words, 0, sizeof(unsigned) * (1 + (size_t)pl->tiles_fb), ctx->stream));
   }
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  return NNGP_OK;
+}
+
+int nngp_bf_primary(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  if (t1 > pl->tiles) t1 = pl->tiles;
+  if (t0 < 0) t0 = 0;
+  if (t1 <= t0) return NNGP_OK;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (ctx->timing) {
-    for (cudaEvent_t *e : {&t0, &t1}) {
+    for (cudaEvent_t *e : {&e0, &e1}) {
       if (!ctx->event_pool.empty()) {
         *e = ctx->event_pool.back();
         ctx->event_pool.pop_back();
@@ -350,23 +374,36 @@ int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
         cudaEventCreate(e);
       }
     }
-    cudaEventRecord(t0, ctx->stream);
+    cudaEventRecord(e0, ctx->stream);
   }
-  if ((st = launch_pass(ctx, pl, fp32r, false))) return st;
+  const int st = launch_pass(ctx, pl, pl->precision == NNGP_FP32R, false, t0, t1);
   if (ctx->timing) {
-    cudaEventRecord(t1, ctx->stream);
-    ctx->timed.emplace_back(t0, t1);
+    cudaEventRecord(e1, ctx->stream);
+    ctx->timed.emplace_back(e0, e1);
   }
+  return st;
+}
+
+int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
+  int st;
+  const bool fp32r = pl->precision == NNGP_FP32R;
   // FP32R: the FP64 re-solve of the recorded tiles, folded into the same fixed-order sums
-  if (fp32r && (st = launch_pass(ctx, pl, false, true))) return st;
+  if (fp32r && (st = launch_pass(ctx, pl, false, true, 0, 0))) return st;
   reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr,
                                                              fp32r ? pl->d_fb_words + 1 : nullptr, pl->ng, d_out);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }
 
+int nngp_bf_run(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
+  int st;
+  if ((st = nngp_bf_begin(ctx, pl))) return st;
+  if ((st = nngp_bf_primary(ctx, pl, 0, pl->tiles))) return st;
+  return nngp_bf_finish(ctx, pl, d_out);
+}
+
 int nngp_bf_launch(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass) {
-  return launch_pass(ctx, pl, fp32r, fallback_pass);
+  return launch_pass(ctx, pl, fp32r, fallback_pass, 0, pl->tiles);
 }
 
 void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *pl) {
@@ -437,10 +474,19 @@ int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches) {
 }
 
 namespace {
-__global__ void prepare_coords_kernel(const double *__restrict__ cm, int n, double *__restrict__ xy,
-                                      float *__restrict__ xyf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__global__ void split_v_kernel(const double *__restrict__ V, int64_t count, float2 *__restrict__ Vf) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) {
+    const double v = V[t];
+    const float h = (float)v;
+    Vf[t] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+__global__ void prepare_coords_kernel(const double *__restrict__ cm, int n, int i0, int i1,
+                                      double *__restrict__ xy, float *__restrict__ xyf) {
+  const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= i1) return;
   const double x = cm[i], y = cm[n + i];
   if (xy) {
     xy[2 * i] = x;
@@ -453,17 +499,6 @@ __global__ void prepare_coords_kernel(const double *__restrict__ cm, int n, doub
 }
 }  // namespace
 
-namespace {
-__global__ void split_v_kernel(const double *__restrict__ V, int64_t count, float2 *__restrict__ Vf) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < count) {
-    const double v = V[t];
-    const float h = (float)v;
-    Vf[t] = make_float2(h, (float)(v - (double)h));
-  }
-}
-}  // namespace
-
 int nngp_split_v(nngp_ctx *ctx, const double *V, int64_t count, float2 *Vf) {
   if (count <= 0) return NNGP_OK;
   split_v_kernel<<<(unsigned)((count + 255) / 256), 256, 0, ctx->stream>>>(V, count, Vf);
@@ -471,9 +506,10 @@ int nngp_split_v(nngp_ctx *ctx, const double *V, int64_t count, float2 *Vf) {
   return NNGP_OK;
 }
 
-int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf) {
-  if (n <= 0) return NNGP_OK;
-  prepare_coords_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(cm, n, xy, xyf);
+int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf, int i0, int i1) {
+  if (i1 < 0 || i1 > n) i1 = n;
+  if (i1 <= i0) return NNGP_OK;
+  prepare_coords_kernel<<<(i1 - i0 + 255) / 256, 256, 0, ctx->stream>>>(cm, n, i0, i1, xy, xyf);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }

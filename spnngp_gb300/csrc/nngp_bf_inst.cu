@@ -6,6 +6,6 @@
 #error "nngp_bf_inst.cu is compiled once per variant with -DBF_M, -DBF_R32 and -DBF_COV"
 #endif
 namespace nngp_bf {
-template int launch_one<BF_M, (BF_R32 != 0), 0, BF_COV>(nngp_ctx *, const BFPlan *, bool);
-template int launch_one<BF_M, (BF_R32 != 0), 1, BF_COV>(nngp_ctx *, const BFPlan *, bool);
+template int launch_one<BF_M, (BF_R32 != 0), 0, BF_COV>(nngp_ctx *, const BFPlan *, bool, int, int);
+template int launch_one<BF_M, (BF_R32 != 0), 1, BF_COV>(nngp_ctx *, const BFPlan *, bool, int, int);
 }  // namespace nngp_bf

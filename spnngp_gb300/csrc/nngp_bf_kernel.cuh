@@ -108,7 +108,7 @@ template <int M, bool R32, int MODE, int TPB, int COV>
 __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ datas,
                                                  const CovParams *__restrict__ thetas,
                                                  const BFJob *__restrict__ jobs, int njobs,
-                                                 int total_tiles, int nv,
+                                                 int tile_begin, int tile_end, int nv,
                                                  unsigned long long *__restrict__ status,
                                                  int only_flagged, const int *__restrict__ tile_list,
                                                  const int *__restrict__ tile_count) {
@@ -127,10 +127,10 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
 #define GEO_(k, q) geo[(size_t)((k) * GEO + (q)) * TPB + tid]
 
   // the FP64 re-solve walks the list of tiles the FP32R pass recorded; the other passes walk
-  // every tile
-  const int ntodo = tile_list ? *tile_count : total_tiles;
+  // tiles [tile_begin, tile_end)
+  const int ntodo = tile_list ? *tile_count : tile_end - tile_begin;
   for (int kt = blockIdx.x; kt < ntodo; kt += gridDim.x) {
-    const int tile = tile_list ? tile_list[kt] : kt;
+    const int tile = tile_list ? tile_list[kt] : tile_begin + kt;
     const int jid = find_job(jobs, njobs, tile);
     const BFJob job = jobs[jid];
     const BFData d = datas[job.data];
@@ -432,7 +432,7 @@ constexpr int bf_tpb() {
 }
 
 template <int M, bool R32, int MODE, int COV>
-int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass) {
+int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1) {
   constexpr int TPB = bf_tpb<M, R32>();
   using T = typename std::conditional<R32, float, double>::type;
   constexpr int GEO = R32 ? 4 : 2;
@@ -444,7 +444,7 @@ int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass) {
     NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = true;
   }
-  const int tiles = fallback_pass ? pl->tiles_fb : pl->tiles;
+  const int tiles = fallback_pass ? pl->tiles_fb : t1 - t0;
   const BFJob *jobs = fallback_pass ? pl->d_jobs_fb : pl->d_jobs;
   if (tiles <= 0) return NNGP_OK;
   // the re-solve pass: a grid of about two blocks per SM walks the recorded tiles (none
@@ -454,7 +454,8 @@ int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass) {
     const int cap = 2 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
     grid = tiles < cap ? tiles : cap;
   }
-  kern<<<grid, TPB, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, jobs, pl->njobs, tiles, pl->nv,
+  kern<<<grid, TPB, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, jobs, pl->njobs,
+                                         fallback_pass ? 0 : t0, fallback_pass ? pl->tiles_fb : t1, pl->nv,
                                          pl->d_status, fallback_pass ? 1 : 0,
                                          fallback_pass ? pl->d_fb_list : nullptr,
                                          fallback_pass ? (const int *)pl->d_fb_words : nullptr);

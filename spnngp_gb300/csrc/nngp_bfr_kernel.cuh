@@ -147,7 +147,7 @@ template <int M, int MODE, int COV>
 __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ datas,
                                                      const CovParams *__restrict__ thetas,
                                                      const BFJob *__restrict__ jobs, int njobs,
-                                                     int total_tiles, int nv) {
+                                                     int tile_begin, int tile_end, int nv) {
   using S = Shape<M>;
   namespace F = nngp_df;
   extern __shared__ __align__(16) float smem_f[];
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
 #define CLV(e) wv[(S::NC + (e)) * 32 + lane]
   constexpr int kStage = 2 * NNGP_MAX_NV;  // first staging slot of the per-warp sums
 
-  for (int tile = blockIdx.x * wpb + warp; tile < total_tiles; tile += gridDim.x * wpb) {
+  for (int tile = tile_begin + blockIdx.x * wpb + warp; tile < tile_end; tile += gridDim.x * wpb) {
     const BFJob job = jobs[find_job(jobs, njobs, tile)];
     const BFData d = datas[job.data];
     const CovParams *cpp = thetas + job.theta;
@@ -411,13 +411,14 @@ cudaError_t configure(int device) {
   return e;
 }
 
-// Launches the kernel on the plan's primary jobs with wpb warps per block and `grid` blocks.
+// Launches the kernel on the plan's primary tiles [t0, t1) with wpb warps per block and `grid`
+// blocks.
 template <int M, int MODE, int COV>
-int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid) {
+int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1) {
   NNGP_CUDA_TRY(ctx, (configure<M, MODE, COV>(ctx->device)));
-  if (pl->tiles <= 0) return NNGP_OK;
+  if (t1 <= t0) return NNGP_OK;
   bfr_kernel<M, MODE, COV><<<grid, 32 * wpb, smem_bytes<M>(wpb), ctx->stream>>>(
-      pl->d_datas, pl->d_thetas, pl->d_jobs, pl->njobs, pl->tiles, pl->nv);
+      pl->d_datas, pl->d_thetas, pl->d_jobs, pl->njobs, t0, t1, pl->nv);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }

@@ -120,6 +120,11 @@ void nngp_destroy(nngp_ctx *ctx) {
     cudaEventDestroy(pr.second);
   }
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->chunk_events) cudaEventDestroy(e);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }

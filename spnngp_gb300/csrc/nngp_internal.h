@@ -67,6 +67,10 @@ struct nngp_ctx {
   bool autotune = true;
   int force_wpb = 0, force_grid_mode = 0;
   std::map<std::string, TuneEntry> tuned;
+  // host-pointer entry points stream their inputs in on this stream, chunk by chunk, while
+  // the context stream computes (created on first use)
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> chunk_events;
 };
 void nngp_bf_cache_release(nngp_ctx *ctx);
 
@@ -231,6 +235,16 @@ int nngp_bf_launch(nngp_ctx *ctx, const BFPlan *plan, bool fp32r, bool fallback_
 // Launches the pass; d_out receives njobs x ng sums (log F first, then the Gram
 // entries r_a r_b / F over a <= b, row-major).
 int nngp_bf_run(nngp_ctx *ctx, const BFPlan *plan, double *d_out);
+// The same pass in pieces, for callers that stream their inputs in: begin (clears the FP32R
+// flags), the primary kernel over tiles [t0, t1) as often as needed to cover every tile
+// (tile = location / nngp_bf_tile(precision, m) of a single-job plan), then finish (FP64
+// re-solve of flagged locations and the fixed-order sums).  Results are identical to
+// nngp_bf_run's.
+int nngp_bf_begin(nngp_ctx *ctx, const BFPlan *plan);
+int nngp_bf_primary(nngp_ctx *ctx, const BFPlan *plan, int t0, int t1);
+int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *plan, double *d_out);
+// Locations per primary tile of a plan with this precision and largest m.
+int nngp_bf_tile(int precision, int mmax);
 void nngp_bf_plan_free(nngp_ctx *ctx, BFPlan *plan);
 // Stream-ordered device allocation (pooled), freed with nngp_free_async.
 void *nngp_malloc_async(nngp_ctx *ctx, size_t bytes);
@@ -263,8 +277,10 @@ constexpr int nngp_bfr_max_wpb(int M) {
 int nngp_split_v(nngp_ctx *ctx, const double *V, int64_t count, float2 *Vf);
 
 // Writes the interleaved double coordinates (xy, may be null) and their float hi/lo
-// split (xyf, may be null) from the n x 2 column-major coordinates.
-int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf);
+// split (xyf, may be null) from the n x 2 column-major coordinates, for locations
+// [i0, i1) (default: all).
+int nngp_prepare_coords(nngp_ctx *ctx, const double *cm, int n, double *xy, float *xyf, int i0 = 0,
+                        int i1 = -1);
 
 // Device status word: 0xFFFF..FF = ok, otherwise (code << 48) | location.
 constexpr unsigned long long NNGP_STATUS_OK = ~0ull;

@@ -357,10 +357,11 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
   // Instances are split into classes by neighbor bound and by correlation code -- the model,
   // with Matern needing the general-nu kernel when nu is sampled or starts off the
   // half-integers -- so each class runs the kernel instantiation it needs and no other.  The
-  // bounds are those the kernels are built for: FP32R 10 / 15 / 16 (register kernel) and 32;
-  // FP64 16 and 32.
-  constexpr int NCLS = 20;
+  // bounds are those the kernels are built for: FP32R 10 / 15 / 16 (register kernel), 24 and
+  // 32; FP64 16, 24 and 32.
+  constexpr int NCLS = 25;
   auto bound_class = [&](int m) {
+    if (m > 24) return 4;
     if (m > 16) return 3;
     if (precision != NNGP_FP32R) return 2;
     return m <= 10 ? 0 : (m <= 15 ? 1 : 2);
@@ -445,21 +446,51 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
       }
     return NNGP_OK;
   };
-  auto run_cur = [&]() -> int {
-    for (int c = 0; c < NCLS; c++)
-      if (haveCur[c]) {
-        const int r = nngp_bf_run(ctx, &planCur[c], d_out0c[c]);
-        if (r) return r;
-      }
-    return NNGP_OK;
-  };
   // initial state: likelihood pass at the starting theta (candidate slot = start)
   st = run_cand();
   if (!st) {
     mc_init_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
     ctx->launches++;
   }
-  // one iteration as a graph (with and without the replicate draw)
+  // one iteration as a graph (with and without the replicate draw).  The classes' passes are
+  // independent: each class runs on its own branch (side streams forked from and joined back
+  // to the capturing stream), so small classes overlap instead of queueing.
+  int nclasses = 0;
+  for (int c = 0; c < NCLS; c++) nclasses += haveCand[c] ? 1 : 0;
+  const int nside = nclasses > 1 ? (nclasses < 4 ? nclasses : 4) : 0;
+  cudaStream_t side[4] = {};
+  cudaEvent_t evFork = nullptr, evJoin[NCLS] = {};
+  bool branches_ok = nside > 0;
+  for (int k = 0; k < nside && branches_ok; k++)
+    branches_ok = cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking) == cudaSuccess;
+  if (branches_ok) branches_ok = cudaEventCreateWithFlags(&evFork, cudaEventDisableTiming) == cudaSuccess;
+  for (int c = 0; c < NCLS && branches_ok; c++)
+    if (haveCand[c]) branches_ok = cudaEventCreateWithFlags(&evJoin[c], cudaEventDisableTiming) == cudaSuccess;
+  // runs run_one(c) for every class, on parallel branches when they are available
+  auto fan_out = [&](auto run_one) -> int {
+    if (!branches_ok) {
+      for (int c = 0; c < NCLS; c++)
+        if (haveCand[c]) {
+          const int r = run_one(c);
+          if (r) return r;
+        }
+      return NNGP_OK;
+    }
+    cudaStream_t main_stream = ctx->stream;
+    if (cudaEventRecord(evFork, main_stream) != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, "graph fork");
+    int r = NNGP_OK, k = 0;
+    for (int c = 0; c < NCLS && !r; c++) {
+      if (!haveCand[c]) continue;
+      cudaStream_t sc = side[k++ % nside];
+      cudaStreamWaitEvent(sc, evFork, 0);
+      ctx->stream = sc;
+      r = run_one(c);
+      ctx->stream = main_stream;
+      cudaEventRecord(evJoin[c], sc);
+      cudaStreamWaitEvent(main_stream, evJoin[c], 0);
+    }
+    return r;
+  };
   auto capture = [&](bool rep, cudaGraphExec_t *exec) -> int {
     cudaGraph_t g;
     const cudaError_t eb = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
@@ -467,10 +498,10 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     int s2 = NNGP_OK;
     mc_pre_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
     if (rep) {
-      s2 = run_cur();
+      s2 = fan_out([&](int c) { return haveCur[c] ? nngp_bf_run(ctx, &planCur[c], d_out0c[c]) : NNGP_OK; });
       mc_rep_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
     }
-    if (!s2) s2 = run_cand();
+    if (!s2) s2 = fan_out([&](int c) { return nngp_bf_run(ctx, &planCand[c], d_outc[c]); });
     mc_post_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (s2) return s2;
@@ -504,6 +535,11 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) st = nngp_fail(ctx, NNGP_ERR_CUDA, std::string("mcmc: ") + cudaGetErrorString(e));
   }
+  for (int k = 0; k < nside; k++)
+    if (side[k]) cudaStreamDestroy(side[k]);
+  if (evFork) cudaEventDestroy(evFork);
+  for (int c = 0; c < NCLS; c++)
+    if (evJoin[c]) cudaEventDestroy(evJoin[c]);
   if (gPlain) cudaGraphExecDestroy(gPlain);
   if (gRep) cudaGraphExecDestroy(gRep);
   if (!st) st = nngp_check_status(ctx, d_status, "rNNGP");

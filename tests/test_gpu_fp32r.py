@@ -104,10 +104,18 @@ def test_launch_shape_does_not_change_results(sp, orc, m):
     assert ldt == ref[3][0] and np.array_equal(Gt, ref[4])
 
 
-def test_autotune_reports_choice(sp, orc):
+def test_autotune_reports_choice(sp):
+    """A pass of at least 2048 tiles (64 K locations) is tuned once per class; smaller ones run
+    the default shape untuned."""
     ctx = sp.Context(0)
-    c, X, y = dataset(20000, 77)
-    o = orc.mkNNIndxCB(cm(c), 15)
+    small = dataset(20000, 76)
+    nbs = sp.mkNNIndxCB(small[0], 15, ctx=ctx)
+    sp.loglik_gram(small[0], nbs["nnIndx"], nbs["nnIndxLU"], 15, np.column_stack(small[1:]), "gaussian",
+                   (1.0, 0.1, 5.0), "fp32r", ctx=ctx)
+    assert ctx.autotune_report() == {}
+    c, X, y = dataset(100_000, 77)
+    nb = sp.mkNNIndxCB(c, 15, ctx=ctx)
+    o = (nb["nnIndx"], None, nb["nnIndxLU"])
     V = np.column_stack([X, y])
     sp.loglik_gram(c, o[0], o[2], 15, V, "gaussian", (1.0, 0.1, 5.0), "fp32r", ctx=ctx)
     rep = ctx.autotune_report()
@@ -120,3 +128,42 @@ def test_autotune_reports_choice(sp, orc):
     sp.loglik_gram(c, o[0], o[2], 15, V, "gaussian", (1.0, 0.1, 5.0), "fp32r", ctx=ctx)
     assert ctx.autotune_report() == rep
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32r", "fp64"])
+def test_streamed_host_form_matches_resident_form(sp, precision):
+    """The host-pointer entry points stream their inputs in location chunks (n = 300k: 2 chunks)
+    and launch the pass tile range by tile range; results are bitwise those of the
+    device-pointer form, which runs the pass in one launch."""
+    import ctypes as C
+
+    import torch
+
+    from spnngp_gb300._lib import _dp
+
+    n, m, nv = 300_000, 15, 3
+    c, X, y = dataset(n, 91, nv)
+    nb = sp.mkNNIndxCB(c, m)
+    nn, lu = nb["nnIndx"], nb["nnIndxLU"]
+    V = np.column_stack([X, y])
+    theta = (1.0, 0.1, 30.0)
+    ld_h, G_h = sp.loglik_gram(c, nn, lu, m, V, "exponential", theta, precision)
+    B_h, F_h, ldb_h = sp.updateBF(c, nn, lu, m, "exponential", theta, precision)
+    ctx = sp.default_context()
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    d_c, d_nn, d_lu, d_V = t(cm(c)), t(nn), t(lu), t(cm(V))
+    d_ld = torch.zeros(1, dtype=torch.float64, device=dev)
+    d_G = torch.zeros(nv * nv, dtype=torch.float64, device=dev)
+    th = np.array(list(theta) + [0.0])
+    prec = 1 if precision == "fp32r" else 0
+    ctx.call("nngp_loglik_gram_dev", n, m, nv, d_c.data_ptr(), d_nn.data_ptr(), d_lu.data_ptr(), d_V.data_ptr(), 0,
+             th.ctypes.data_as(_dp), prec, d_ld.data_ptr(), d_G.data_ptr())
+    assert d_ld.item() == ld_h
+    assert np.array_equal(d_G.cpu().numpy().reshape(nv, nv), G_h)
+    d_B = torch.zeros(len(nn), dtype=torch.float64, device=dev)
+    d_F = torch.zeros(n, dtype=torch.float64, device=dev)
+    ctx.call("nngp_updateBF_dev", n, m, d_c.data_ptr(), d_nn.data_ptr(), d_lu.data_ptr(), 0, th.ctypes.data_as(_dp),
+             prec, d_B.data_ptr(), d_F.data_ptr(), d_ld.data_ptr())
+    assert np.array_equal(d_B.cpu().numpy(), B_h) and np.array_equal(d_F.cpu().numpy(), F_h)
+    assert d_ld.item() == ldb_h
