@@ -462,7 +462,9 @@ def run_ours(args):
     if args.launch_shape:
         w, g = (int(v) for v in args.launch_shape.split(","))
         ctx.set_launch_shape(w, g)
-    stream = torch.cuda.current_stream(dev)
+    # one stream for torch's work (uploads, L2 flush, timing events) and the library's kernels
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     import ctypes as C
 

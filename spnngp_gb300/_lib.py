@@ -176,7 +176,15 @@ class Context:
         return st
 
     def set_stream(self, stream_handle: int | None):
-        self._lib.fn("nngp_set_stream")(self.handle, stream_handle or None)
+        """Launch on this cudaStream_t handle; None = the context's own (non-blocking) stream.
+
+        Handle 0 is CUDA's legacy default stream (torch's default stream), which the C ABI cannot
+        name (NULL selects the context's own stream): work on it would not be ordered with this
+        library's.  Share a torch.cuda.Stream() instead."""
+        if stream_handle is not None and int(stream_handle) == 0:
+            raise ValueError("stream handle 0 (the legacy default stream) cannot be shared with the library; "
+                             "use a torch.cuda.Stream() (and make it current) or None for the context's own stream")
+        self._lib.fn("nngp_set_stream")(self.handle, stream_handle)
 
     def synchronize(self):
         self.call("nngp_synchronize")

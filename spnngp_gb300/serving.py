@@ -108,7 +108,9 @@ class ConjServer:
         self.torch = torch
         self.ctx = ctx or default_context()
         self.dev = torch.device("cuda", self.ctx.device)
-        self.stream = torch.cuda.current_stream(self.dev)
+        # one stream for the server's torch work (uploads, ordering, output buffers) and the
+        # library's kernels, so each sees the other's results in order
+        self.stream = torch.cuda.Stream(self.dev)
         self.ctx.set_stream(self.stream.cuda_stream)
         self.m = m
         self.model = cov_model_index(cov_model)
@@ -195,6 +197,11 @@ class ConjServer:
     # -------------------------------------------------------------- iteration
     def step(self, now=time.perf_counter) -> list:
         """One serving iteration: admit, prepare, one batched fit + predict, retire."""
+        self.ctx.set_stream(self.stream.cuda_stream)  # the context may be shared with other callers
+        with self.torch.cuda.stream(self.stream):
+            return self._step(now)
+
+    def _step(self, now) -> list:
         torch = self.torch
         batch = self._admit()
         if not batch:

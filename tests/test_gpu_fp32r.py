@@ -157,12 +157,14 @@ def test_streamed_host_form_matches_resident_form(sp, precision):
     d_G = torch.zeros(nv * nv, dtype=torch.float64, device=dev)
     th = np.array(list(theta) + [0.0])
     prec = 1 if precision == "fp32r" else 0
+    torch.cuda.synchronize()  # the library runs on its own stream
     ctx.call("nngp_loglik_gram_dev", n, m, nv, d_c.data_ptr(), d_nn.data_ptr(), d_lu.data_ptr(), d_V.data_ptr(), 0,
              th.ctypes.data_as(_dp), prec, d_ld.data_ptr(), d_G.data_ptr())
     assert d_ld.item() == ld_h
     assert np.array_equal(d_G.cpu().numpy().reshape(nv, nv), G_h)
     d_B = torch.zeros(len(nn), dtype=torch.float64, device=dev)
     d_F = torch.zeros(n, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
     ctx.call("nngp_updateBF_dev", n, m, d_c.data_ptr(), d_nn.data_ptr(), d_lu.data_ptr(), 0, th.ctypes.data_as(_dp),
              prec, d_B.data_ptr(), d_F.data_ptr(), d_ld.data_ptr())
     assert np.array_equal(d_B.cpu().numpy(), B_h) and np.array_equal(d_F.cpu().numpy(), F_h)

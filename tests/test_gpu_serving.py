@@ -123,3 +123,30 @@ def test_serve_replays_stream(sp):
     out = serve(ConjServer(), reqs)
     assert out["completed"] == 12 and out["failed"] == 0
     assert out["p50_s"] > 0 and out["p99_s"] >= out["p50_s"]
+
+
+def test_cached_datasets_match_fresh_builds(sp):
+    """Datasets a server builds back to back in one batch (torch sorts and gathers the
+    coordinates, the library searches neighbors) are identical to fresh builds, and the served
+    results equal the per-request form bitwise.  Guards the ordering between torch's work and
+    the library's kernels."""
+    import torch
+
+    from spnngp_gb300.serving import ConjServer, fit_predict_one
+
+    rng = np.random.default_rng(12)
+    reqs = [make_request(rng, n, 2000, rid=k, dataset=k) for k, n in enumerate([60000, 25000, 90000, 40000, 15000])]
+    srv = ConjServer(precision="fp64")
+    for r in reqs:
+        srv.submit(r)
+    got = {r.rid: r for r in srv.drain()}
+    torch.cuda.synchronize()
+    for r in reqs:
+        fresh = ConjServer(precision="fp64")
+        f = fresh._dataset(r, "fresh")
+        torch.cuda.synchronize()
+        for name in ("coords", "X", "y", "nn", "lu"):
+            assert torch.equal(srv.datasets[r.dataset].tensors[name], f.tensors[name]), (r.rid, name)
+        ref = fit_predict_one(r, precision="fp64")
+        for fld in FIELDS:
+            assert np.array_equal(getattr(got[r.rid], fld), getattr(ref, fld)), (r.rid, fld)

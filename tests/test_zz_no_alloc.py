@@ -70,6 +70,7 @@ def _alloc(t, n, m, nv, model, theta):
     ld = torch.zeros(1, dtype=torch.float64, device="cuda")
     G = torch.zeros(nv * nv, dtype=torch.float64, device="cuda")
     th = np.array(list(theta) + [0.0] * (4 - len(theta)))
+    torch.cuda.synchronize()  # the context runs on its own stream, not torch's
     ctx.call("nngp_loglik_gram_dev", n, m, nv, t["c"].data_ptr(), t["nn"].data_ptr(), t["lu"].data_ptr(),
              t["V"].data_ptr(), model, th.ctypes.data_as(_dp), 0, ld.data_ptr(), G.data_ptr())
     out = (ld.item(), G.cpu().numpy().reshape(nv, nv))
