@@ -60,6 +60,18 @@ struct Shape {
 };
 __host__ __device__ constexpr int lidx(int r, int c) { return r * (r - 1) / 2 + c; }  // r > c
 
+// (r, c) of strict-lower-triangle entry e in storage order, packed r << 8 | c (M <= 16); read
+// warp-uniformly, so the build loop's iterations carry no dependency through the indices
+struct PairTable {
+  unsigned short rc[120];
+  constexpr PairTable() : rc() {
+    int e = 0;
+    for (int r = 1; r < 16; r++)
+      for (int c = 0; c < r; c++) rc[e++] = (unsigned short)(r << 8 | c);
+  }
+};
+static __constant__ PairTable kPairs = PairTable();
+
 // Per-tile constants of the correlation function in double-float.
 struct CorDF {
   nngp_df::df K;   // exp argument scale in units of ln2/32: -phi 32/ln2 (times d), gaussian -phi^2 32/ln2 (times d^2)
@@ -70,23 +82,20 @@ struct CorDF {
   int model;
 };
 
+// Reads the parameter set's prepared double-float constants (cov_prepare): no FP64 here.
 template <int COV>
 __device__ __forceinline__ CorDF cor_prepare(const CovParams *cp) {
-  namespace F = nngp_df;
   CorDF k{};
-  const int model = COV == NNGP_COV_ANY ? cp->model : COV;
-  k.model = model;
+  k.model = COV == NNGP_COV_ANY ? cp->model : COV;
   k.halfk = cp->halfk;
-  k.P = F::from_double(cp->phi);
-  k.S2 = F::from_double(cp->sigmaSq);
-  const double c32 = 46.166241308446828;  // 32 / ln 2
-  k.K = F::from_double(model == 3 ? -(cp->phi * cp->phi) * c32 : -cp->phi * c32);
-  if (model == 2 && cp->halfk >= 0) {
+  k.K = nngp_df::df{cp->dfK[0], cp->dfK[1]};
+  k.P = nngp_df::df{cp->dfPhi[0], cp->dfPhi[1]};
+  k.S2 = nngp_df::df{cp->dfS2[0], cp->dfS2[1]};
+  if (COV == NNGP_COV_MAT_HALF || (COV == NNGP_COV_ANY && k.model == 2 && k.halfk >= 0)) {
 #pragma unroll
     for (int j = 0; j < 9; j++) {
-      const F::df c = F::from_double(cp->poly[j]);
-      k.pfh[j] = c.h;
-      k.pfl[j] = c.l;
+      k.pfh[j] = cp->dfPoly[j][0];
+      k.pfl[j] = cp->dfPoly[j][1];
     }
   }
   return k;
@@ -133,6 +142,19 @@ __device__ __forceinline__ nngp_df::df cov_df(nngp_df::df d2, const CorDF &k, co
   return F::mul(E, s);
 }
 
+// Models whose correlation is one exp of a scaled distance take the packed path: two pairs per
+// instruction stream (Blackwell f32x2), same arithmetic as cov_df.
+template <int COV>
+constexpr bool kPacked = COV == NNGP_COV_EXP || COV == NNGP_COV_GAU;
+
+template <int COV>
+__device__ __forceinline__ nngp_df2::df2 cov_df2(nngp_df2::df2 d2, const CorDF &k, const float *tab) {
+  namespace G = nngp_df2;
+  const G::df2 K{G::splat(k.K.h), G::splat(k.K.l)};
+  if constexpr (COV == NNGP_COV_GAU) return G::exp_u(G::mul(K, d2), tab);
+  else return G::exp_u(G::mul(K, G::sqrt(d2)), tab);
+}
+
 __device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) {
   int lo = 0, hi = njobs - 1;
   while (lo < hi) {
@@ -177,9 +199,8 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
       off = d.nnLU[i];
       mi = min(d.nnLU[d.n + i], M);
     }
-    const double sigmaSq = cpp->sigmaSq, tauSq = cpp->tauSq;
     const CorDF ck = cor_prepare<COV>(cpp);
-    const F::df Sd = F::from_double(sigmaSq + tauSq);  // the diagonal sigma^2 + tau^2
+    const F::df Sd{cpp->dfDiag[0], cpp->dfDiag[1]};  // the diagonal sigma^2 + tau^2
     {  // the warp's exp table: sigma^2 2^(j/32)
       const float2 t2 = F::kExp2Tab[lane];
       const F::df e = F::mul(ck.S2, F::df{t2.x, t2.y});
@@ -188,40 +209,115 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
     }
     __syncwarp();
 
-    // ---- 1. geometry
+    // ---- 1. geometry: offsets from the location as double-float pairs whose hi parts lie on a
+    // common grid 2^e with 2^e >= 2^-22 max|offset|, so the hi parts of two offsets subtract
+    // exactly (at most 24 bits) and a pair difference needs no error-free transformation
     const float4 *xyf = reinterpret_cast<const float4 *>(d.xyf);
     const float4 pi4 = active ? xyf[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    F::df ox[M], oy[M];
+    float omax = 1e-30f;
 #pragma unroll
     for (int k = 0; k < M; k++) {
+      ox[k] = oy[k] = F::df{0.0f, 0.0f};
       if (k < mi) {
         const float4 q = xyf[d.nnIndx[off + k]];
-        const F::df ox = F::diff(q.x, q.z, pi4.x, pi4.z), oy = F::diff(q.y, q.w, pi4.y, pi4.w);
-        GEO(k) = make_float4(ox.h, oy.h, ox.l, oy.l);
+        ox[k] = F::diff(q.x, q.z, pi4.x, pi4.z);
+        oy[k] = F::diff(q.y, q.w, pi4.y, pi4.w);
+        omax = fmaxf(omax, fmaxf(fabsf(ox[k].h), fabsf(oy[k].h)));
+      }
+    }
+    {
+      const int eb = ((__float_as_int(omax) >> 23) & 0xff) - 22;  // biased exponent of 2^e
+      const float grid = __int_as_float(max(eb, 1) << 23), inv = __int_as_float((254 - max(eb, 1)) << 23);
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        if (k < mi) {
+          const float hx = __fmul_rn(rintf(__fmul_rn(ox[k].h, inv)), grid);
+          const float hy = __fmul_rn(rintf(__fmul_rn(oy[k].h, inv)), grid);
+          GEO(k) = make_float4(hx, hy, __fadd_rn(__fsub_rn(ox[k].h, hx), ox[k].l),
+                               __fadd_rn(__fsub_rn(oy[k].h, hy), oy[k].l));
+        }
       }
     }
     // ---- 2. covariance build (rolled), double-float: the c vector, then the strict lower
-    // triangle as one loop over its pairs in storage order (four independent pairs in flight)
-#pragma unroll 4
-    for (int r = 0; r < mi; r++) {
-      const float4 g = GEO(r);
-      const F::df cr = cov_df<COV>(F::sumsq(g.x, g.z, g.y, g.w), ck, tab, cpp);
-      CS(S::NL + r) = cr.h;
-      CL(S::NL + r) = cr.l;
+    // triangle as one loop over its pairs in storage order.  Each step handles four pairs with
+    // all loads first, then the four (independent) evaluations, then the stores: shared-memory
+    // stores and loads through one base pointer may alias as far as the compiler knows, so a
+    // plain unrolled loop would run its iterations one after another.
+#pragma unroll 1
+    for (int r0 = 0; r0 < mi; r0 += 4) {
+      float4 g[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) g[j] = GEO(min(r0 + j, mi - 1));
+      F::df v[4];
+      if constexpr (kPacked<COV>) {
+        namespace G = nngp_df2;
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+          G::df2 gx, gy;
+          G::two_sum(G::pack(g[2 * t].x, g[2 * t + 1].x), G::pack(g[2 * t].z, g[2 * t + 1].z), gx.h, gx.l);
+          G::two_sum(G::pack(g[2 * t].y, g[2 * t + 1].y), G::pack(g[2 * t].w, g[2 * t + 1].w), gy.h, gy.l);
+          const G::df2 r = cov_df2<COV>(G::sumsq(gx, gy), ck, tab);
+          v[2 * t] = F::df{G::first(r.h), G::first(r.l)};
+          v[2 * t + 1] = F::df{G::second(r.h), G::second(r.l)};
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const F::df gx = F::norm(g[j].x, g[j].z), gy = F::norm(g[j].y, g[j].w);
+          v[j] = cov_df<COV>(F::sumsq(gx.h, gx.l, gy.h, gy.l), ck, tab, cpp);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (r0 + j < mi) {
+          CS(S::NL + r0 + j) = v[j].h;
+          CL(S::NL + r0 + j) = v[j].l;
+        }
     }
     {
       const int npairs = mi * (mi - 1) / 2;
-      int r = 1, c = 0;
-#pragma unroll 4
-      for (int e = 0; e < npairs; e++) {
-        const float4 g = GEO(r), h = GEO(c);
-        const F::df ex = F::diff(g.x, g.z, h.x, h.z), ey = F::diff(g.y, g.w, h.y, h.w);
-        const F::df v = cov_df<COV>(F::sumsq(ex.h, ex.l, ey.h, ey.l), ck, tab, cpp);
-        CS(e) = v.h;  // e == lidx(r, c)
-        CL(e) = v.l;
-        if (++c == r) {
-          r++;
-          c = 0;
+#pragma unroll 1
+      for (int e0 = 0; e0 < npairs; e0 += 4) {
+        float4 g[4], h[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int rc = kPairs.rc[min(e0 + j, npairs - 1)];
+          g[j] = GEO(rc >> 8);
+          h[j] = GEO(rc & 255);
         }
+        F::df v[4];
+        if constexpr (kPacked<COV>) {
+          namespace G = nngp_df2;
+#pragma unroll
+          for (int t = 0; t < 2; t++) {
+            const int a = 2 * t, b2 = 2 * t + 1;
+            // hi parts on the common grid: their difference is exact
+            G::df2 ex, ey;
+            G::fast_two_sum(G::sub(G::pack(g[a].x, g[b2].x), G::pack(h[a].x, h[b2].x)),
+                            G::sub(G::pack(g[a].z, g[b2].z), G::pack(h[a].z, h[b2].z)), ex.h, ex.l);
+            G::fast_two_sum(G::sub(G::pack(g[a].y, g[b2].y), G::pack(h[a].y, h[b2].y)),
+                            G::sub(G::pack(g[a].w, g[b2].w), G::pack(h[a].w, h[b2].w)), ey.h, ey.l);
+            const G::df2 r = cov_df2<COV>(G::sumsq(ex, ey), ck, tab);
+            v[a] = F::df{G::first(r.h), G::first(r.l)};
+            v[b2] = F::df{G::second(r.h), G::second(r.l)};
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            // hi parts on the common grid: their difference is exact
+            F::df ex, ey;
+            F::fast_two_sum(__fsub_rn(g[j].x, h[j].x), __fsub_rn(g[j].z, h[j].z), ex.h, ex.l);
+            F::fast_two_sum(__fsub_rn(g[j].y, h[j].y), __fsub_rn(g[j].w, h[j].w), ey.h, ey.l);
+            v[j] = cov_df<COV>(F::sumsq(ex.h, ex.l, ey.h, ey.l), ck, tab, cpp);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (e0 + j < npairs) {
+            CS(e0 + j) = v[j].h;  // e == lidx(r, c)
+            CL(e0 + j) = v[j].l;
+          }
       }
     }
 #pragma unroll 1
@@ -279,21 +375,55 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
     for (int r = 0; r < M; r++) w[r] = 0.0f;
 #pragma unroll
     for (int r = 0; r < M; r++) {
-      float sh = 0.0f, sl = 0.0f;
+      // C[r][c] b[c] over c, even and odd c in the two halves of a packed compensated sum (the
+      // 16-neighbor bound keeps the scalar sum: its registers are full)
+      namespace G = nngp_df2;
+      if constexpr (M >= 16) {
+        float shs = 0.0f, sls = 0.0f;
 #pragma unroll
-      for (int c = 0; c < M; c++) {
-        float eh, el;
-        if (c == r) {
-          eh = (r < mi) ? Sd.h : 1.0f;
-          el = (r < mi) ? Sd.l : 0.0f;
-        } else {
-          eh = c < r ? CSV(lidx(r, c)) : CSV(lidx(c, r));
-          el = c < r ? CLV(lidx(r, c)) : CLV(lidx(c, r));
+        for (int c = 0; c < M; c++) {
+          float eh, el;
+          if (c == r) {
+            eh = (r < mi) ? Sd.h : 1.0f;
+            el = (r < mi) ? Sd.l : 0.0f;
+          } else {
+            eh = c < r ? CSV(lidx(r, c)) : CSV(lidx(c, r));
+            el = c < r ? CLV(lidx(r, c)) : CLV(lidx(c, r));
+          }
+          F::dot2_acc(shs, sls, eh, b[c]);
+          sls = fmaf(el, b[c], sls);
         }
-        F::dot2_acc(sh, sl, eh, b[c]);
-        sl = fmaf(el, b[c], sl);
+        const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), shs), sls), CLV(S::NL + r));
+        w[r] = (res - w[r]) * D[r];
+#pragma unroll
+        for (int j = r + 1; j < M; j++) w[j] = fmaf(L[lidx(j, r)], w[r], w[j]);
+        continue;
       }
-      const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), sh), sl), CLV(S::NL + r));
+      G::p2 sh = 0ull, sl = 0ull;
+#pragma unroll
+      for (int c0 = 0; c0 < M; c0 += 2) {
+        float eh[2], el[2], bc[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+          const int c = c0 + u;
+          eh[u] = el[u] = bc[u] = 0.0f;
+          if (c < M) {
+            bc[u] = b[c];
+            if (c == r) {
+              eh[u] = (r < mi) ? Sd.h : 1.0f;
+              el[u] = (r < mi) ? Sd.l : 0.0f;
+            } else {
+              eh[u] = c < r ? CSV(lidx(r, c)) : CSV(lidx(c, r));
+              el[u] = c < r ? CLV(lidx(r, c)) : CLV(lidx(c, r));
+            }
+          }
+        }
+        const G::p2 b2 = G::pack(bc[0], bc[1]);
+        G::dot2_acc(sh, sl, G::pack(eh[0], eh[1]), b2);
+        sl = G::fma(G::pack(el[0], el[1]), b2, sl);
+      }
+      const F::df cb = G::fold(sh, sl);
+      const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), cb.h), cb.l), CLV(S::NL + r));
       w[r] = (res - w[r]) * D[r];
 #pragma unroll
       for (int j = r + 1; j < M; j++) w[j] = fmaf(L[lidx(j, r)], w[r], w[j]);
@@ -307,16 +437,29 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
     // B = b + w (unevaluated float pair)
 
     // ---- 5. F, error estimate, log F, likelihood terms
-    float dh = 0.0f, dl = 0.0f, bmax = 0.0f, wmax = 0.0f;
+    float bmax = 0.0f, wmax = 0.0f;
+    F::df bc;
+    {
+      namespace G = nngp_df2;
+      G::p2 dh = 0ull, dl = 0ull;
 #pragma unroll
-    for (int k = 0; k < M; k++) {
-      const float ch = CSV(S::NL + k), cl = CLV(S::NL + k);
-      F::dot2_acc(dh, dl, b[k], ch);
-      dl = fmaf(w[k], ch, fmaf(b[k], cl, dl));
-      bmax = fmaxf(bmax, fabsf(b[k]));
-      wmax = fmaxf(wmax, fabsf(w[k]));
+      for (int k0 = 0; k0 < M; k0 += 2) {
+        const int k1 = k0 + 1 < M ? k0 + 1 : k0;
+        const float z1 = k0 + 1 < M ? 1.0f : 0.0f;  // the odd half of the last step is empty
+        const G::p2 ch = G::pack(CSV(S::NL + k0), z1 * CSV(S::NL + k1));
+        const G::p2 cl = G::pack(CLV(S::NL + k0), z1 * CLV(S::NL + k1));
+        const G::p2 bb = G::pack(b[k0], z1 * b[k1]), ww = G::pack(w[k0], z1 * w[k1]);
+        G::dot2_acc(dh, dl, bb, ch);
+        dl = G::fma(ww, ch, G::fma(bb, cl, dl));
+      }
+      bc = G::fold(dh, dl);
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        bmax = fmaxf(bmax, fabsf(b[k]));
+        wmax = fmaxf(wmax, fabsf(w[k]));
+      }
     }
-    const F::df Fd = F::sub(Sd, F::norm(dh, dl));
+    const F::df Fd = F::sub(Sd, F::norm(bc.h, bc.l));
     const float q = wmax / fmaxf(bmax, 1e-30f);
     const bool bad = !ok || !(Fd.h > kMinFRel * Sd.h) || !(q * q * Sd.h <= kTolF * Fd.h);
     if (active && bad) nngp_flag_for_fp64(job, i);
@@ -336,22 +479,39 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
 #pragma unroll
       for (int k = 0; k < M; k++) nb[k] = (k < mi) ? d.nnIndx[off + k] : 0;
       const float2 *Vf = d.Vf;
-      // r_v = V_iv - sum_k B_k V_nb(k)v, staged at slots 2v, 2v + 1
+      // r_v = V_iv - sum_k B_k V_nb(k)v, staged at slots 2v, 2v + 1.  Four columns at a time:
+      // all of a group's gathers are issued before their first use (one memory round trip
+      // per group instead of one per column; the factor's registers are free by now)
 #pragma unroll 1
-      for (int v = 0; v < nv; v++) {
-        float ah = 0.0f, al = 0.0f;
+      for (int v0 = 0; v0 < nv; v0 += 4) {
+        float2 q[4][M], vi[4];
 #pragma unroll
-        for (int k = 0; k < M; k++) {
-          if (k < mi) {
-            const float2 q = Vf[(size_t)nb[k] * nv + v];
-            F::dot2_acc(ah, al, b[k], q.x);
-            al = fmaf(b[k], q.y, fmaf(w[k], q.x, al));
+        for (int j = 0; j < 4; j++) {
+#pragma unroll
+          for (int k = 0; k < M; k++)
+            q[j][k] = (k < mi && v0 + j < nv) ? Vf[(size_t)nb[k] * nv + v0 + j] : make_float2(0.f, 0.f);
+          vi[j] = (active && v0 + j < nv) ? Vf[(size_t)i * nv + v0 + j] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (v0 + j < nv) {
+            namespace G = nngp_df2;
+            G::p2 ah = 0ull, al = 0ull;
+#pragma unroll
+            for (int k0 = 0; k0 < M; k0 += 2) {
+              const int k1 = k0 + 1 < M ? k0 + 1 : k0;
+              const float z1 = k0 + 1 < M ? 1.0f : 0.0f;
+              const G::p2 bb = G::pack(b[k0], z1 * b[k1]), ww = G::pack(w[k0], z1 * w[k1]);
+              const G::p2 qh = G::pack(q[j][k0].x, q[j][k1].x), ql = G::pack(q[j][k0].y, q[j][k1].y);
+              G::dot2_acc(ah, al, bb, qh);
+              al = G::fma(bb, ql, G::fma(ww, qh, al));
+            }
+            const F::df s2 = G::fold(ah, al);
+            const F::df rv = F::sub(F::df{vi[j].x, vi[j].y}, F::norm(s2.h, s2.l));
+            CS(2 * (v0 + j)) = rv.h;
+            CS(2 * (v0 + j) + 1) = rv.l;
           }
         }
-        const float2 vi = active ? Vf[(size_t)i * nv + v] : make_float2(0.f, 0.f);
-        const F::df rv = F::sub(F::df{vi.x, vi.y}, F::norm(ah, al));
-        CS(2 * v) = rv.h;
-        CS(2 * v + 1) = rv.l;
       }
       const F::df invF = use ? F::recip(Fd) : F::df{0.0f, 0.0f};
       CS(kStage) = lf.h;

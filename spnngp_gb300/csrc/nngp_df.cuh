@@ -220,3 +220,141 @@ __device__ __forceinline__ df diff(float ah, float al, float bh, float bl) {
 }
 
 }  // namespace nngp_df
+
+// ------------------------------------------------------------ packed pairs (f32x2)
+// Two independent double-float computations in lockstep: each 64-bit register holds one float
+// of each (Blackwell's packed FP32 add/sub/mul/fma, round to nearest, issue one instruction
+// for both).  The error-free transformations are the scalar ones above, applied per half.
+namespace nngp_df2 {
+
+typedef unsigned long long p2;  // (lo half, hi half) = (first computation, second)
+
+__device__ __forceinline__ p2 pack(float a, float b) {
+  p2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float first(p2 a) {
+  float x, y;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a));
+  return x;
+}
+__device__ __forceinline__ float second(p2 a) {
+  float x, y;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a));
+  return y;
+}
+__device__ __forceinline__ p2 add(p2 a, p2 b) {
+  p2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ p2 sub(p2 a, p2 b) {
+  p2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ p2 mul(p2 a, p2 b) {
+  p2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ p2 fma(p2 a, p2 b, p2 c) {
+  p2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ p2 neg(p2 a) { return a ^ 0x8000000080000000ull; }
+__device__ __forceinline__ p2 splat(float a) { return pack(a, a); }
+
+struct df2 {
+  p2 h, l;
+};
+
+__device__ __forceinline__ void two_sum(p2 a, p2 b, p2 &s, p2 &e) {
+  s = add(a, b);
+  const p2 bv = sub(s, a);
+  const p2 av = sub(s, bv);
+  e = add(sub(a, av), sub(b, bv));
+}
+__device__ __forceinline__ void fast_two_sum(p2 a, p2 b, p2 &s, p2 &e) {
+  s = add(a, b);
+  e = sub(b, sub(s, a));
+}
+// (a.h + a.l)(b.h + b.l), normalised
+__device__ __forceinline__ df2 mul(df2 a, df2 b) {
+  const p2 p = mul(a.h, b.h);
+  p2 e = fma(a.h, b.h, neg(p));
+  e = fma(a.h, b.l, fma(a.l, b.h, e));
+  df2 r;
+  fast_two_sum(p, e, r.h, r.l);
+  return r;
+}
+// x^2 + y^2 for normalised double-float x, y
+__device__ __forceinline__ df2 sumsq(df2 x, df2 y) {
+  const p2 p1 = mul(x.h, x.h);
+  p2 e1 = fma(x.h, x.h, neg(p1));
+  e1 = fma(add(x.h, x.h), x.l, e1);
+  const p2 p2_ = mul(y.h, y.h);
+  p2 e2 = fma(y.h, y.h, neg(p2_));
+  e2 = fma(add(y.h, y.h), y.l, e2);
+  p2 s, q;
+  two_sum(p1, p2_, s, q);
+  df2 r;
+  fast_two_sum(s, add(add(q, e1), e2), r.h, r.l);
+  return r;
+}
+// sqrt(a) for a >= 0 (0 at 0): float estimate and one Newton correction in the low part
+__device__ __forceinline__ df2 sqrt(df2 a) {
+  const p2 rs = pack(rsqrtf(fmaxf(first(a.h), 1e-37f)), rsqrtf(fmaxf(second(a.h), 1e-37f)));
+  const p2 y = mul(a.h, rs);
+  const p2 yy = mul(y, y), yye = fma(y, y, neg(yy));
+  const p2 num = add(sub(sub(a.h, yy), yye), a.l);  // a.h - yy is exact
+  df2 r;
+  fast_two_sum(y, mul(num, mul(splat(0.5f), rs)), r.h, r.l);
+  return r;
+}
+
+// Dot2 step on both halves: hi + lo += x * y (each half its own compensated sum)
+__device__ __forceinline__ void dot2_acc(p2 &hi, p2 &lo, p2 x, p2 y) {
+  const p2 p = mul(x, y);
+  const p2 pe = fma(x, y, neg(p));
+  p2 q;
+  two_sum(hi, p, hi, q);
+  lo = add(lo, add(q, pe));
+}
+// The two halves of a packed compensated sum added into one double-float (hi exact, lo
+// rounded: the result carries the accuracy of either half)
+__device__ __forceinline__ nngp_df::df fold(p2 hi, p2 lo) {
+  float s, e;
+  nngp_df::two_sum(first(hi), second(hi), s, e);
+  return nngp_df::df{s, __fadd_rn(e, __fadd_rn(first(lo), second(lo)))};
+}
+
+// The scalar exp_u of nngp_df (Tang's table-driven exp in double-float) for two arguments:
+// scale * e^(u ln2/32), u <= 0, the table tab[j] = scale 2^(j/32) (hi at j, lo at 32 + j).
+__device__ __forceinline__ df2 exp_u(df2 u, const float *tab) {
+  const float u0 = fmaxf(first(u.h), -1846.0f), u1 = fmaxf(second(u.h), -1846.0f);
+  const float n0f = rintf(u0), n1f = rintf(u1);
+  const int n0 = (int)n0f, n1 = (int)n1f;
+  p2 ruh, rul;
+  fast_two_sum(sub(pack(u0, u1), pack(n0f, n1f)), u.l, ruh, rul);
+  const p2 c1h = splat(nngp_df::kLn2Over32Hi), c1l = splat(nngp_df::kLn2Over32Lo);
+  const p2 rh = mul(ruh, c1h);
+  const p2 rl = fma(ruh, c1l, fma(rul, c1h, fma(ruh, c1h, neg(rh))));
+  const p2 q = mul(rh, rh), qe = fma(rh, rh, neg(q));
+  p2 poly = fma(rh, splat(1.0f / 120.0f), splat(1.0f / 24.0f));
+  poly = fma(rh, poly, splat(1.0f / 6.0f));
+  const p2 tail = fma(mul(q, rh), poly, fma(rh, rl, fma(splat(0.5f), qe, rl)));
+  p2 s, e, s2, e2;
+  fast_two_sum(splat(1.0f), rh, s, e);
+  two_sum(s, mul(splat(0.5f), q), s2, e2);
+  const df2 E{s2, add(add(e, e2), tail)};
+  const int j0 = n0 & 31, j1 = n1 & 31, k0 = n0 >> 5, k1 = n1 >> 5;
+  const df2 T{pack(tab[j0], tab[j1]), pack(tab[32 + j0], tab[32 + j1])};
+  const df2 R = mul(E, T);
+  const p2 sc = pack(__int_as_float((k0 + 127) << 23), __int_as_float((k1 + 127) << 23));
+  return df2{mul(R.h, sc), mul(R.l, sc)};
+}
+
+}  // namespace nngp_df2

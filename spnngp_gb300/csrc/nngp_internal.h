@@ -118,13 +118,30 @@ struct CovParams {
   double poly[9];
   int model;
   int halfk;
+  // the FP32R register kernel's constants as double-float (hi, lo) pairs: the exp argument
+  // scale in units of ln2/32 (-phi 32/ln2, gaussian -phi^2 32/ln2), phi, sigma^2,
+  // sigma^2 + tau^2, and the Matern polynomial
+  float dfK[2], dfPhi[2], dfS2[2], dfDiag[2];
+  float dfPoly[9][2];
 };
 
-// Fills mconst / halfk / poly from model and nu.  Callable on host and device.
+__host__ __device__ inline void cov_split(double v, float (&out)[2]) {
+  out[0] = (float)v;
+  out[1] = (float)(v - (double)out[0]);
+}
+
+// Fills mconst / halfk / poly from model and nu, and the double-float constants.  Callable on
+// host and device.
 __host__ __device__ inline void cov_prepare(CovParams &c) {
   c.halfk = -1;
   c.mconst = 0.0;
   for (int j = 0; j < 9; j++) c.poly[j] = 0.0;
+  const double c32 = 46.166241308446828;  // 32 / ln 2
+  cov_split(c.model == 3 ? -(c.phi * c.phi) * c32 : -c.phi * c32, c.dfK);
+  cov_split(c.phi, c.dfPhi);
+  cov_split(c.sigmaSq, c.dfS2);
+  cov_split(c.sigmaSq + c.tauSq, c.dfDiag);
+  for (int j = 0; j < 9; j++) c.dfPoly[j][0] = c.dfPoly[j][1] = 0.0f;
   if (c.model != 2) return;
   c.mconst = 1.0 / (pow(2.0, c.nu - 1.0) * tgamma(c.nu));
   const double k = c.nu - 0.5;
@@ -140,6 +157,7 @@ __host__ __device__ inline void cov_prepare(CovParams &c) {
       const int pw = K - j;
       c.poly[pw] = lead * fact[K + j] / (fact[j] * fact[K - j]) * ldexp(1.0, pw);
     }
+    for (int j = 0; j < 9; j++) cov_split(c.poly[j], c.dfPoly[j]);
   }
 }
 
