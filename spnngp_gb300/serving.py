@@ -168,6 +168,12 @@ class ConjServer:
 
     # ------------------------------------------------------------ preparation
     def _dataset(self, req, key):
+        # torch's work and the library's neighbor search must share the server's stream
+        self.ctx.set_stream(self.stream.cuda_stream)
+        with self.torch.cuda.stream(self.stream):
+            return self._dataset_on_stream(req, key)
+
+    def _dataset_on_stream(self, req, key):
         torch = self.torch
         d = self.datasets.get(key)
         if d is not None:
