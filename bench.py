@@ -460,8 +460,8 @@ def run_ours(args):
 
     ctx = Context(dev.index)
     if args.launch_shape:
-        w, g = (int(v) for v in args.launch_shape.split(","))
-        ctx.set_launch_shape(w, g)
+        parts = [int(v) for v in args.launch_shape.split(",")]
+        ctx.set_launch_shape(parts[0], parts[1], bool(parts[2]) if len(parts) > 2 else False)
     # one stream for torch's work (uploads, L2 flush, timing events) and the library's kernels
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
@@ -653,7 +653,8 @@ def run_ours(args):
                                  "algorithmic_bytes_per_solve": algorithmic_bytes(M, nv),
                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
                          "fp64_pipe_peak_tflops": pk64.value / 1e12},
-            "autotune": {k: {"wpb": v["wpb"], "grid_mode": v["grid_mode"], "ms": v["ms"]} for k, v in tune.items()},
+            "autotune": {k: {"wpb": v["wpb"], "grid_mode": v["grid_mode"], "tmem": v["tmem"], "ms": v["ms"]}
+                         for k, v in tune.items()},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
@@ -675,8 +676,9 @@ def main():
                     help="comma-separated extra workloads reported beside the headline (mcmc, conj, serve), or ''")
     ap.add_argument("--mcmc-iters", type=int, default=200)
     ap.add_argument("--launch-shape", default="",
-                    help="W,G: run the FP32R register kernel with W warps per block and grid mode G "
-                         "instead of the autotuned shape (results are identical for every shape)")
+                    help="W,G[,T]: run the FP32R register kernel with W warps per block, grid mode G and "
+                         "(T = 1) the tensor-memory layout instead of the autotuned shape (results are "
+                         "identical for every shape)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     args.sections = [x for x in args.sections.split(",") if x]

@@ -262,19 +262,22 @@ int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches);
 /* Launch-shape autotuner of the FP32R B/F kernel for m <= 16, no counterpart
  * in the reference (it stands in for the reference's n.omp.threads tuning).
  * The first pass of a (neighbor bound, mode, correlation model, size class)
- * times every candidate shape -- warps per block 1/2/4/8 x one tile per warp
- * or a persistent grid of 1 or 2 x resident blocks x SMs -- on the caller's
- * own data and keeps the fastest for the context; passes under stream capture
- * use the tuned shape, or the default (4 warps, one tile per warp) when none is
- * tuned yet.  Results are identical for every shape (each warp reduces its own
- * 32 locations and the sums are combined in a fixed order), so tuning never
- * changes a result.  nngp_set_autotune(ctx, 0) turns tuning off (default
- * shape); nngp_set_launch_shape forces a shape (wpb 0 = back to tuning);
- * nngp_autotune_report writes one line per tuned class ("key: wpb=W grid_mode=G
- * ms=T | WxBLOCKS:ms WxBLOCKS:ms ...", one entry per candidate shape) into buf
- * and returns the number of classes. */
+ * times every candidate shape -- warps per block 1-6 (8) with the covariance
+ * kept in shared memory, or 4 / 8 with its low-order parts in the SM's tensor
+ * memory, each as one tile per warp or a persistent grid of 1 or 2 x resident
+ * blocks x SMs -- on the caller's own data (at most 64K tiles of it) and keeps
+ * the fastest for the context; passes under stream capture, and passes of
+ * fewer than 2048 tiles, use the tuned shape or the default (4 warps, shared
+ * memory, one tile per warp).  Results are identical for every shape (each
+ * warp reduces its own 32 locations and the sums are combined in a fixed
+ * order), so tuning never changes a result.  nngp_set_autotune(ctx, 0) turns
+ * tuning off (default shape); nngp_set_launch_shape forces a shape (wpb 0 =
+ * back to tuning; use_tmem is honoured for m in 11..16); nngp_autotune_report
+ * writes one line per tuned class ("key: wpb=W grid_mode=G tmem=T ms=X |
+ * WxBLOCKS[t]:ms ...", one entry per candidate, t marking tensor memory) into
+ * buf and returns the number of classes. */
 int nngp_set_autotune(nngp_ctx *ctx, int on);
-int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode);
+int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode, int use_tmem);
 int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len);
 
 /* No counterpart in the reference.  The FP64 fused likelihood pass of

@@ -63,7 +63,7 @@ _SIGNATURES = {
     "nngp_set_kernel_timing": (_i, [_vp, _i]),
     "nngp_kernel_time": (_i, [_vp, _dp, C.POINTER(_i64)]),
     "nngp_set_autotune": (_i, [_vp, _i]),
-    "nngp_set_launch_shape": (_i, [_vp, _i, _i]),
+    "nngp_set_launch_shape": (_i, [_vp, _i, _i, _i]),
     "nngp_autotune_report": (_i, [_vp, C.c_char_p, _i]),
 }
 
@@ -199,12 +199,13 @@ class Context:
     def set_autotune(self, on: bool):
         self.call("nngp_set_autotune", 1 if on else 0)
 
-    def set_launch_shape(self, warps_per_block: int, grid_mode: int = 0):
-        """Forces the FP32R register kernel's launch shape (warps_per_block 0: autotune again)."""
-        self.call("nngp_set_launch_shape", int(warps_per_block), int(grid_mode))
+    def set_launch_shape(self, warps_per_block: int, grid_mode: int = 0, tmem: bool = False):
+        """Forces the FP32R register kernel's launch shape (warps_per_block 0: autotune again);
+        tmem selects the variant keeping the covariance's low-order parts in tensor memory."""
+        self.call("nngp_set_launch_shape", int(warps_per_block), int(grid_mode), 1 if tmem else 0)
 
     def autotune_report(self) -> dict:
-        """Tuned launch shapes: {class: {"wpb", "grid_mode", "ms", "candidates": {"WxBLOCKS": ms}}}."""
+        """Tuned launch shapes: {class: {"wpb", "grid_mode", "tmem", "ms", "candidates": {"WxBLOCKS[t]": ms}}}."""
         buf = C.create_string_buffer(1 << 16)
         self._lib.fn("nngp_autotune_report")(self.handle, buf, len(buf))
         out = {}
@@ -212,7 +213,8 @@ class Context:
             head, _, cands = line.partition(" | ")
             key, _, rest = head.partition(": ")
             kv = dict(t.split("=") for t in rest.split())
-            out[key] = {"wpb": int(kv["wpb"]), "grid_mode": int(kv["grid_mode"]), "ms": float(kv["ms"]),
+            out[key] = {"wpb": int(kv["wpb"]), "grid_mode": int(kv["grid_mode"]), "tmem": int(kv["tmem"]),
+                        "ms": float(kv["ms"]),
                         "candidates": {c.split(":")[0]: float(c.split(":")[1]) for c in cands.split()}}
         return out
 

@@ -20,9 +20,9 @@ constexpr int bf_tpb() {
 }  // namespace nngp_bf
 namespace nngp_bfr {
 template <int M, int MODE, int COV>
-int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1);
+int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1, int tm);
 template <int M, int MODE, int COV>
-int occupancy(int wpb);
+int occupancy(int wpb, int tm);
 }  // namespace nngp_bfr
 using namespace nngp_bf;
 
@@ -91,43 +91,43 @@ int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass,
 // ---------------------------------------------------------------- register kernel
 // Calls launch_reg (query_occ false) or occupancy (true) of the plan's instantiation.
 template <int M, int MODE>
-int reg_call_m(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ, int t0, int t1) {
+int reg_call_m(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ, int t0, int t1, int tm) {
   using namespace nngp_bfr;
   switch (pl->cov) {
     case NNGP_COV_EXP:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_EXP>(wpb) : launch_reg<M, MODE, NNGP_COV_EXP>(ctx, pl, wpb, grid, t0, t1);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_EXP>(wpb, tm) : launch_reg<M, MODE, NNGP_COV_EXP>(ctx, pl, wpb, grid, t0, t1, tm);
     case NNGP_COV_SPH:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_SPH>(wpb) : launch_reg<M, MODE, NNGP_COV_SPH>(ctx, pl, wpb, grid, t0, t1);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_SPH>(wpb, tm) : launch_reg<M, MODE, NNGP_COV_SPH>(ctx, pl, wpb, grid, t0, t1, tm);
     case NNGP_COV_MAT_HALF:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_MAT_HALF>(wpb)
-                       : launch_reg<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, wpb, grid, t0, t1);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_MAT_HALF>(wpb, tm)
+                       : launch_reg<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, wpb, grid, t0, t1, tm);
     case NNGP_COV_GAU:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_GAU>(wpb) : launch_reg<M, MODE, NNGP_COV_GAU>(ctx, pl, wpb, grid, t0, t1);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_GAU>(wpb, tm) : launch_reg<M, MODE, NNGP_COV_GAU>(ctx, pl, wpb, grid, t0, t1, tm);
     default:
-      return query_occ ? occupancy<M, MODE, NNGP_COV_ANY>(wpb) : launch_reg<M, MODE, NNGP_COV_ANY>(ctx, pl, wpb, grid, t0, t1);
+      return query_occ ? occupancy<M, MODE, NNGP_COV_ANY>(wpb, tm) : launch_reg<M, MODE, NNGP_COV_ANY>(ctx, pl, wpb, grid, t0, t1, tm);
   }
 }
-int reg_call(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ, int t0 = 0, int t1 = 0) {
+int reg_call(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, bool query_occ, int t0, int t1, int tm) {
   const bool m1 = pl->mode == 1;
   switch (pl->reg_m) {
     case 10:
-      return m1 ? reg_call_m<10, 1>(ctx, pl, wpb, grid, query_occ, t0, t1)
-                : reg_call_m<10, 0>(ctx, pl, wpb, grid, query_occ, t0, t1);
+      return m1 ? reg_call_m<10, 1>(ctx, pl, wpb, grid, query_occ, t0, t1, tm)
+                : reg_call_m<10, 0>(ctx, pl, wpb, grid, query_occ, t0, t1, tm);
     case 15:
-      return m1 ? reg_call_m<15, 1>(ctx, pl, wpb, grid, query_occ, t0, t1)
-                : reg_call_m<15, 0>(ctx, pl, wpb, grid, query_occ, t0, t1);
+      return m1 ? reg_call_m<15, 1>(ctx, pl, wpb, grid, query_occ, t0, t1, tm)
+                : reg_call_m<15, 0>(ctx, pl, wpb, grid, query_occ, t0, t1, tm);
     default:
-      return m1 ? reg_call_m<16, 1>(ctx, pl, wpb, grid, query_occ, t0, t1)
-                : reg_call_m<16, 0>(ctx, pl, wpb, grid, query_occ, t0, t1);
+      return m1 ? reg_call_m<16, 1>(ctx, pl, wpb, grid, query_occ, t0, t1, tm)
+                : reg_call_m<16, 0>(ctx, pl, wpb, grid, query_occ, t0, t1, tm);
   }
 }
 
 // Blocks of the launch shape (wpb, grid_mode) for this plan: grid_mode 0 gives every warp one
 // tile; k > 0 caps the grid at k x (resident blocks per SM) x SMs, each warp looping over tiles.
-int reg_grid(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid_mode, int ntiles) {
+int reg_grid(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid_mode, int ntiles, int tm) {
   const int full = (ntiles + wpb - 1) / wpb;
   if (grid_mode <= 0) return full > 0 ? full : 1;
-  const int occ = reg_call(ctx, pl, wpb, 0, true);
+  const int occ = reg_call(ctx, pl, wpb, 0, true, 0, 0, tm);
   const long cap = (long)grid_mode * occ * (ctx->sm_count > 0 ? ctx->sm_count : 1);
   return (int)(cap < full ? cap : full);
 }
@@ -145,7 +145,11 @@ std::string tune_key(const BFPlan *pl, int ntiles) {
 // Times every candidate shape on the plan itself (each run rewrites the same outputs with
 // the same values: the results do not depend on the shape) and keeps the fastest.
 int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best, int t0, int t1) {
-  static const int kWpb[] = {1, 2, 3, 4, 5, 6, 8};
+  // shared-memory layouts: 1-6 (8) warps per block; tensor-memory layout: 4 or 8 warps
+  struct Cand {
+    int wpb, tm;
+  };
+  static const Cand kCand[] = {{1, 0}, {2, 0}, {3, 0}, {4, 0}, {5, 0}, {6, 0}, {8, 0}, {4, 1}, {8, 1}};
   static const int kGrid[] = {0, 1, 2};
   cudaEvent_t e0, e1;
   NNGP_CUDA_TRY(ctx, cudaEventCreate(&e0));
@@ -154,15 +158,19 @@ int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best, int t0, int t1) {
   best.ms = 1e30;
   std::string detail;
   int st = NNGP_OK;
-  for (int wpb : kWpb) {
-    if (wpb > nngp_bfr_max_wpb(pl->reg_m)) continue;
-    const int full = reg_grid(ctx, pl, wpb, 0, t1 - t0);
+  for (const Cand &cd : kCand) {
+    const int wpb = cd.wpb, tm = cd.tm;
+    if (tm ? !nngp_bfr_has_tm(pl->reg_m) || wpb > nngp_bfr_max_wpb(pl->reg_m, true)
+           : wpb > nngp_bfr_max_wpb(pl->reg_m, false))
+      continue;
+    if (reg_call(ctx, pl, wpb, 0, true, 0, 0, tm) <= 0) continue;  // no block of this shape fits
+    const int full = reg_grid(ctx, pl, wpb, 0, t1 - t0, tm);
     for (int gm : kGrid) {
-      const int grid = reg_grid(ctx, pl, wpb, gm, t1 - t0);
+      const int grid = reg_grid(ctx, pl, wpb, gm, t1 - t0, tm);
       if (gm > 0 && grid >= full) continue;  // same as the one-tile-per-warp grid
-      if ((st = reg_call(ctx, pl, wpb, grid, false, t0, t1))) break;  // warm-up
+      if ((st = reg_call(ctx, pl, wpb, grid, false, t0, t1, tm))) break;  // warm-up
       cudaEventRecord(e0, ctx->stream);
-      if ((st = reg_call(ctx, pl, wpb, grid, false, t0, t1))) break;
+      if ((st = reg_call(ctx, pl, wpb, grid, false, t0, t1, tm))) break;
       cudaEventRecord(e1, ctx->stream);
       if (cudaEventSynchronize(e1) != cudaSuccess) {
         st = nngp_fail(ctx, NNGP_ERR_CUDA, "autotune: event synchronisation failed");
@@ -171,12 +179,13 @@ int tune_reg(nngp_ctx *ctx, const BFPlan *pl, TuneEntry &best, int t0, int t1) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
       char buf[64];
-      snprintf(buf, sizeof buf, "%s%dx%d:%.4f", detail.empty() ? "" : " ", wpb, grid, ms);
+      snprintf(buf, sizeof buf, "%s%dx%d%s:%.4f", detail.empty() ? "" : " ", wpb, grid, tm ? "t" : "", ms);
       detail += buf;
       if (ms < best.ms) {
         best.ms = ms;
         best.wpb = wpb;
         best.grid_mode = gm;
+        best.tm = tm;
       }
     }
     if (st) break;
@@ -193,16 +202,18 @@ constexpr int kTuneMinTiles = 2048;
 constexpr int kTuneSampleTiles = 65536;
 
 int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
-  int wpb = 4, gm = 0;
+  int wpb = 4, gm = 0, tm = 0;
   if (ctx->force_wpb > 0) {
     wpb = ctx->force_wpb;
     gm = ctx->force_grid_mode;
+    tm = ctx->force_tm && nngp_bfr_has_tm(pl->reg_m) ? 1 : 0;
   } else {
     const std::string key = tune_key(pl, t1 - t0);
     auto it = ctx->tuned.find(key);
     if (it != ctx->tuned.end()) {
       wpb = it->second.wpb;
       gm = it->second.grid_mode;
+      tm = it->second.tm;
     } else if (ctx->autotune && t1 - t0 >= kTuneMinTiles) {
       cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
       cudaStreamIsCapturing(ctx->stream, &cs);
@@ -215,12 +226,17 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
         ctx->tuned[key] = e;
         wpb = e.wpb;
         gm = e.grid_mode;
+        tm = e.tm;
       }
     }
   }
-  const int wmax = nngp_bfr_max_wpb(pl->reg_m);
-  if (wpb > wmax) wpb = wmax;  // a forced shape larger than the block limit of this bound
-  return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm, t1 - t0), false, t0, t1);
+  if (tm) {
+    wpb = wpb > 4 ? 8 : 4;  // the tensor-memory layout runs 4 or 8 warps per block
+  } else {
+    const int wmax = nngp_bfr_max_wpb(pl->reg_m);
+    if (wpb > wmax) wpb = wmax;  // a forced shape larger than the block limit of this bound
+  }
+  return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm, t1 - t0, tm), false, t0, t1, tm);
 }
 
 // Primary pass over tiles [t0, t1), or (fallback_pass) the FP64 re-solve of the recorded tiles.
@@ -426,12 +442,13 @@ int nngp_set_autotune(nngp_ctx *ctx, int on) {
   ctx->autotune = on != 0;
   return NNGP_OK;
 }
-int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode) {
+int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode, int use_tmem) {
   if (!ctx) return NNGP_ERR_ARG;
   if (warps_per_block < 0 || warps_per_block > 8 || grid_mode < 0 || grid_mode > 64)
     return nngp_fail(ctx, NNGP_ERR_ARG, "launch shape: 0 <= warps_per_block <= 8, 0 <= grid_mode <= 64");
   ctx->force_wpb = warps_per_block;
   ctx->force_grid_mode = grid_mode;
+  ctx->force_tm = use_tmem != 0;
   return NNGP_OK;
 }
 int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len) {
@@ -439,8 +456,8 @@ int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len) {
   std::string out;
   for (const auto &kv : ctx->tuned) {
     char line[160];
-    snprintf(line, sizeof line, "%s: wpb=%d grid_mode=%d ms=%.4f | ", kv.first.c_str(), kv.second.wpb,
-             kv.second.grid_mode, kv.second.ms);
+    snprintf(line, sizeof line, "%s: wpb=%d grid_mode=%d tmem=%d ms=%.4f | ", kv.first.c_str(), kv.second.wpb,
+             kv.second.grid_mode, kv.second.tm, kv.second.ms);
     out += line;
     out += kv.second.detail;
     out += "\n";

@@ -6,8 +6,8 @@
 #error "nngp_bfr_inst.cu is compiled once per variant with -DBFR_M and -DBFR_COV"
 #endif
 namespace nngp_bfr {
-template int launch_reg<BFR_M, 0, BFR_COV>(nngp_ctx *, const BFPlan *, int, int, int, int);
-template int launch_reg<BFR_M, 1, BFR_COV>(nngp_ctx *, const BFPlan *, int, int, int, int);
-template int occupancy<BFR_M, 0, BFR_COV>(int);
-template int occupancy<BFR_M, 1, BFR_COV>(int);
+template int launch_reg<BFR_M, 0, BFR_COV>(nngp_ctx *, const BFPlan *, int, int, int, int, int);
+template int launch_reg<BFR_M, 1, BFR_COV>(nngp_ctx *, const BFPlan *, int, int, int, int, int);
+template int occupancy<BFR_M, 0, BFR_COV>(int, int);
+template int occupancy<BFR_M, 1, BFR_COV>(int, int);
 }  // namespace nngp_bfr

@@ -49,15 +49,40 @@ constexpr int kNGMax = 1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2;
 constexpr float kTolF = 1e-8f;    // accepted F error estimate, relative to F
 constexpr float kMinFRel = 1e-6f;  // smaller F (relative to sigma^2 + tau^2) goes to FP64
 
-template <int M>
+// Per-lane layout (floats, each interleaved over the warp's 32 lanes): [0, NL) hi parts of
+// the strict lower triangle, [NL, NC) hi parts of c, [NC, NC + M) lo parts of c, then (without
+// tensor memory) the NL lo parts of the strict lower triangle, then the geometry.  With TM the
+// strict lower triangle's lo parts live in tensor memory instead, as full symmetric rows of 16
+// columns (row r at columns 16 r .. 16 r + 15 of the warp's range), so the residual reads a
+// row with one load.
+template <int M, bool TM = false>
 struct Shape {
   static constexpr int NL = M * (M - 1) / 2;  // strict lower triangle of C
   static constexpr int NC = NL + M;           // ... followed by the c vector
-  static constexpr int LANE = nngp_bfr_lane_floats(M);  // hi parts, lo parts, geometry (or staging)
+  static constexpr int CLO = NC;              // lo parts of c
+  static constexpr int LLO = NC + M;          // lo parts of the strict lower triangle (!TM)
+  static constexpr int GEO = NC + M + (TM ? 0 : NL);
+  static constexpr int LANE = nngp_bfr_lane_floats(M, TM);
   static constexpr int TAB = 64;              // per-warp exp table (32 hi, 32 lo)
-  static constexpr size_t WARP_BYTES = nngp_bfr_warp_bytes(M);
-  static constexpr int MAX_WPB = nngp_bfr_max_wpb(M);
+  static constexpr size_t WARP_BYTES = nngp_bfr_warp_bytes(M, TM);
+  static constexpr int MAX_WPB = nngp_bfr_max_wpb(M, TM);
+  static_assert(GEO + 4 * M <= LANE, "layout exceeds the lane's share");
 };
+
+// Tensor-memory access (tcgen05): one 32-bit value per lane and column.  A warp reaches the
+// lanes of its quarter (32 (warp % 4) ..) only; the caller adds that lane base.
+__device__ __forceinline__ void tm_st(unsigned addr, float v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" ::"r"(addr), "f"(v));
+}
+__device__ __forceinline__ void tm_ld16(unsigned addr, float (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]), "=f"(r[6]), "=f"(r[7]), "=f"(r[8]),
+        "=f"(r[9]), "=f"(r[10]), "=f"(r[11]), "=f"(r[12]), "=f"(r[13]), "=f"(r[14]), "=f"(r[15])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __host__ __device__ constexpr int lidx(int r, int c) { return r * (r - 1) / 2 + c; }  // r > c
 
 // (r, c) of strict-lower-triangle entry e in storage order, packed r << 8 | c (M <= 16); read
@@ -165,26 +190,45 @@ __device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) 
   return lo;
 }
 
-template <int M, int MODE, int COV>
+template <int M, int MODE, int COV, bool TM>
 __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ datas,
                                                      const CovParams *__restrict__ thetas,
                                                      const BFJob *__restrict__ jobs, int njobs,
                                                      int tile_begin, int tile_end, int nv) {
-  using S = Shape<M>;
+  using S = Shape<M, TM>;
   namespace F = nngp_df;
   extern __shared__ __align__(16) float smem_f[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   float *ws = smem_f + (size_t)warp * (32 * S::LANE + S::TAB);
   float *tab = ws + 32 * S::LANE;
-  float4 *geo = reinterpret_cast<float4 *>(ws + 32 * 2 * S::NC);
+  float4 *geo = reinterpret_cast<float4 *>(ws + 32 * S::GEO);
 #define CS(e) ws[(e) * 32 + lane]
-#define CL(e) ws[(S::NC + (e)) * 32 + lane]
+#define CLC(r) ws[(S::CLO + (r)) * 32 + lane]
+#define CLL(e) ws[(S::LLO + (e)) * 32 + lane]
 #define GEO(k) geo[(k) * 32 + lane]
   // C and c are read again after the factorization: volatile reads stop the compiler from
   // keeping the first reads alive in registers beside the factor (which spills)
   volatile float *wv = ws;
 #define CSV(e) wv[(e) * 32 + lane]
-#define CLV(e) wv[(S::NC + (e)) * 32 + lane]
+#define CLCV(r) wv[(S::CLO + (r)) * 32 + lane]
+#define CLLV(e) wv[(S::LLO + (e)) * 32 + lane]
+  // tensor memory (TM): the CTA's warp 0 allocates 256 columns per four warps; warp w owns lane
+  // quarter w % 4 and columns 256 (w / 4) .. + 255 of the allocation
+  __shared__ unsigned tm_alloc_base;
+  unsigned tm0 = 0;
+  const unsigned tm_cols = wpb > 4 ? 512u : 256u;
+  if constexpr (TM) {
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       (unsigned)__cvta_generic_to_shared(&tm_alloc_base)),
+                   "r"(tm_cols));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tm0 = tm_alloc_base + ((32u * (unsigned)(warp & 3)) << 16) + 256u * (unsigned)(warp >> 2);
+  }
   constexpr int kStage = 2 * NNGP_MAX_NV;  // first staging slot of the per-warp sums
 
   for (int tile = tile_begin + blockIdx.x * wpb + warp; tile < tile_end; tile += gridDim.x * wpb) {
@@ -272,19 +316,23 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
       for (int j = 0; j < 4; j++)
         if (r0 + j < mi) {
           CS(S::NL + r0 + j) = v[j].h;
-          CL(S::NL + r0 + j) = v[j].l;
+          CLC(r0 + j) = v[j].l;
         }
     }
     {
-      const int npairs = mi * (mi - 1) / 2;
+      // every lane covers all NL pairs of the bound (a warp-uniform trip count: the tensor-memory
+      // stores are warp-collective); a pair in a padded row (r >= m_i) is stored as 0
 #pragma unroll 1
-      for (int e0 = 0; e0 < npairs; e0 += 4) {
+      for (int e0 = 0; e0 < S::NL; e0 += 4) {
         float4 g[4], h[4];
+        int rr[4], cc[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          const int rc = kPairs.rc[min(e0 + j, npairs - 1)];
-          g[j] = GEO(rc >> 8);
-          h[j] = GEO(rc & 255);
+          const int rc = kPairs.rc[min(e0 + j, S::NL - 1)];
+          rr[j] = rc >> 8;
+          cc[j] = rc & 255;
+          g[j] = GEO(min(rr[j], M - 1));
+          h[j] = GEO(cc[j]);
         }
         F::df v[4];
         if constexpr (kPacked<COV>) {
@@ -313,22 +361,27 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
           }
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++)
-          if (e0 + j < npairs) {
-            CS(e0 + j) = v[j].h;  // e == lidx(r, c)
-            CL(e0 + j) = v[j].l;
+        for (int j = 0; j < 4; j++) {
+          if (e0 + j < S::NL) {
+            const bool live = rr[j] < mi;
+            const float vh = live ? v[j].h : 0.0f, vl = live ? v[j].l : 0.0f;
+            CS(e0 + j) = vh;  // e == lidx(r, c)
+            if constexpr (TM) {
+              tm_st(tm0 + 16u * rr[j] + cc[j], vl);
+              tm_st(tm0 + 16u * cc[j] + rr[j], vl);
+            } else {
+              CLL(e0 + j) = vl;
+            }
           }
+        }
       }
     }
 #pragma unroll 1
-    for (int r = mi; r < M; r++) {  // identity padding
+    for (int r = mi; r < M; r++) {  // identity padding of c
       CS(S::NL + r) = 0.0f;
-      CL(S::NL + r) = 0.0f;
-      float *rowh = &CS(lidx(r, 0));
-      float *rowl = &CL(lidx(r, 0));
-#pragma unroll 1
-      for (int c = 0; c < r; c++) rowh[c * 32] = rowl[c * 32] = 0.0f;
+      CLC(r) = 0.0f;
     }
+    if constexpr (TM) tm_wait_st();
 
     // ---- 3. Cholesky and solves on registers (hi parts)
     float L[S::NL > 0 ? S::NL : 1];
@@ -378,6 +431,8 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
       // C[r][c] b[c] over c, even and odd c in the two halves of a packed compensated sum (the
       // 16-neighbor bound keeps the scalar sum: its registers are full)
       namespace G = nngp_df2;
+      float lo_row[16];
+      if constexpr (TM) tm_ld16(tm0 + 16u * r, lo_row);
       if constexpr (M >= 16) {
         float shs = 0.0f, sls = 0.0f;
 #pragma unroll
@@ -388,12 +443,13 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
             el = (r < mi) ? Sd.l : 0.0f;
           } else {
             eh = c < r ? CSV(lidx(r, c)) : CSV(lidx(c, r));
-            el = c < r ? CLV(lidx(r, c)) : CLV(lidx(c, r));
+            if constexpr (TM) el = lo_row[c];
+            else el = c < r ? CLLV(lidx(r, c)) : CLLV(lidx(c, r));
           }
           F::dot2_acc(shs, sls, eh, b[c]);
           sls = fmaf(el, b[c], sls);
         }
-        const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), shs), sls), CLV(S::NL + r));
+        const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), shs), sls), CLCV(r));
         w[r] = (res - w[r]) * D[r];
 #pragma unroll
         for (int j = r + 1; j < M; j++) w[j] = fmaf(L[lidx(j, r)], w[r], w[j]);
@@ -414,7 +470,8 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
               el[u] = (r < mi) ? Sd.l : 0.0f;
             } else {
               eh[u] = c < r ? CSV(lidx(r, c)) : CSV(lidx(c, r));
-              el[u] = c < r ? CLV(lidx(r, c)) : CLV(lidx(c, r));
+              if constexpr (TM) el[u] = lo_row[c];
+              else el[u] = c < r ? CLLV(lidx(r, c)) : CLLV(lidx(c, r));
             }
           }
         }
@@ -423,7 +480,7 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
         sl = G::fma(G::pack(el[0], el[1]), b2, sl);
       }
       const F::df cb = G::fold(sh, sl);
-      const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), cb.h), cb.l), CLV(S::NL + r));
+      const float res = __fadd_rn(__fsub_rn(__fsub_rn(CSV(S::NL + r), cb.h), cb.l), CLCV(r));
       w[r] = (res - w[r]) * D[r];
 #pragma unroll
       for (int j = r + 1; j < M; j++) w[j] = fmaf(L[lidx(j, r)], w[r], w[j]);
@@ -447,7 +504,7 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
         const int k1 = k0 + 1 < M ? k0 + 1 : k0;
         const float z1 = k0 + 1 < M ? 1.0f : 0.0f;  // the odd half of the last step is empty
         const G::p2 ch = G::pack(CSV(S::NL + k0), z1 * CSV(S::NL + k1));
-        const G::p2 cl = G::pack(CLV(S::NL + k0), z1 * CLV(S::NL + k1));
+        const G::p2 cl = G::pack(CLCV(k0), z1 * CLCV(k1));
         const G::p2 bb = G::pack(b[k0], z1 * b[k1]), ww = G::pack(w[k0], z1 * w[k1]);
         G::dot2_acc(dh, dl, bb, ch);
         dl = G::fma(ww, ch, G::fma(bb, cl, dl));
@@ -546,54 +603,89 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
     }
     __syncwarp();
   }
+  if constexpr (TM) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (warp == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm_alloc_base), "r"(tm_cols));
+  }
 #undef CS
 #undef CSV
-#undef CL
-#undef CLV
+#undef CLC
+#undef CLCV
+#undef CLL
+#undef CLLV
 #undef GEO
 }
 
-template <int M>
+template <int M, bool TM>
 constexpr size_t smem_bytes(int wpb) {
-  return Shape<M>::WARP_BYTES * (size_t)wpb;
+  return Shape<M, TM>::WARP_BYTES * (size_t)wpb;
 }
 
 // Raises the kernel's dynamic shared-memory limit to what the largest block (MAX_WPB warps)
 // needs (once per device; the attribute is per device).
-template <int M, int MODE, int COV>
+template <int M, int MODE, int COV, bool TM>
 cudaError_t configure(int device) {
   static bool configured[64] = {};
   const int dev = device & 63;
   if (configured[dev]) return cudaSuccess;
-  const cudaError_t e = cudaFuncSetAttribute(bfr_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem_bytes<M>(Shape<M>::MAX_WPB));
+  const cudaError_t e = cudaFuncSetAttribute(bfr_kernel<M, MODE, COV, TM>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem_bytes<M, TM>(Shape<M, TM>::MAX_WPB));
   if (e == cudaSuccess) configured[dev] = true;
   return e;
 }
 
-// Launches the kernel on the plan's primary tiles [t0, t1) with wpb warps per block and `grid`
-// blocks.
-template <int M, int MODE, int COV>
-int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1) {
-  NNGP_CUDA_TRY(ctx, (configure<M, MODE, COV>(ctx->device)));
+template <int M, int MODE, int COV, bool TM>
+int launch_tm(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1) {
+  NNGP_CUDA_TRY(ctx, (configure<M, MODE, COV, TM>(ctx->device)));
   if (t1 <= t0) return NNGP_OK;
-  bfr_kernel<M, MODE, COV><<<grid, 32 * wpb, smem_bytes<M>(wpb), ctx->stream>>>(
+  bfr_kernel<M, MODE, COV, TM><<<grid, 32 * wpb, smem_bytes<M, TM>(wpb), ctx->stream>>>(
       pl->d_datas, pl->d_thetas, pl->d_jobs, pl->njobs, t0, t1, pl->nv);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }
 
-// Blocks of wpb warps one SM holds at once (on the current device).
+// Launches the kernel on the plan's primary tiles [t0, t1) with wpb warps per block and `grid`
+// blocks; tm selects the variant with the covariance's lo parts in tensor memory (wpb 4 or 8).
 template <int M, int MODE, int COV>
-int occupancy(int wpb) {
-  if (wpb > Shape<M>::MAX_WPB) return 0;
+int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t1, int tm) {
+  if constexpr (nngp_bfr_has_tm(M)) {
+    if (tm) {
+      if (wpb != 4 && wpb != 8)
+        return nngp_fail(ctx, NNGP_ERR_ARG, "the tensor-memory B/F kernel runs 4 or 8 warps per block");
+      return launch_tm<M, MODE, COV, true>(ctx, pl, wpb, grid, t0, t1);
+    }
+  }
+  return launch_tm<M, MODE, COV, false>(ctx, pl, wpb, grid, t0, t1);
+}
+
+// Blocks of wpb warps one SM holds at once (on the current device); 0 when the shape is not
+// available for this variant.
+template <int M, int MODE, int COV>
+int occupancy(int wpb, int tm) {
   int dev = 0, blocks = 0;
   cudaGetDevice(&dev);
-  if (configure<M, MODE, COV>(dev) != cudaSuccess) return 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, bfr_kernel<M, MODE, COV>, 32 * wpb,
-                                                    smem_bytes<M>(wpb)) != cudaSuccess)
-    return 1;
-  return blocks > 0 ? blocks : 1;
+  if constexpr (nngp_bfr_has_tm(M)) {
+    if (tm) {
+      if (wpb != 4 && wpb != 8) return 0;
+      if (configure<M, MODE, COV, true>(dev) != cudaSuccess) return 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, bfr_kernel<M, MODE, COV, true>, 32 * wpb,
+                                                        smem_bytes<M, true>(wpb)) != cudaSuccess)
+        return 0;
+      // at most 512 tensor-memory columns per SM: 256 per four warps
+      const int tm_cap = wpb == 8 ? 1 : 2;
+      return blocks < tm_cap ? blocks : tm_cap;
+    }
+  }
+  if (tm || wpb > Shape<M, false>::MAX_WPB) return 0;
+  if (configure<M, MODE, COV, false>(dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, bfr_kernel<M, MODE, COV, false>, 32 * wpb,
+                                                    smem_bytes<M, false>(wpb)) != cudaSuccess)
+    return 0;
+  return blocks;
 }
 
 }  // namespace nngp_bfr

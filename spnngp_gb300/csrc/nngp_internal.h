@@ -38,6 +38,7 @@ struct BFPlan;
 struct TuneEntry {
   int wpb = 4;
   int grid_mode = 0;
+  int tm = 0;  // 1: the kernel variant keeping the covariance's lo parts in tensor memory
   double ms = 0.0;
   std::string detail;
 };
@@ -65,7 +66,7 @@ struct nngp_ctx {
   // register B/F kernel launch shapes: autotuned on first use (outside stream capture), or
   // forced by nngp_set_launch_shape (force_wpb > 0)
   bool autotune = true;
-  int force_wpb = 0, force_grid_mode = 0;
+  int force_wpb = 0, force_grid_mode = 0, force_tm = 0;
   std::map<std::string, TuneEntry> tuned;
   // host-pointer entry points stream their inputs in on this stream, chunk by chunk, while
   // the context stream computes (created on first use)
@@ -277,20 +278,27 @@ inline int nngp_reg_m(int precision, int mmax) {
     if (mmax <= M) return M;
   return 0;
 }
-// Shared memory of the register kernel: per lane the double-float covariance (hi and lo
-// parts of the strict lower triangle and the c vector) and one float4 of geometry per
-// neighbor (the epilogue's staging of 2 NNGP_MAX_NV + 2 (1 + NV(NV+1)/2) floats reuses it);
-// per warp a 64-float exp table.  Blocks hold at most 8 warps and 227 KB.
-constexpr int nngp_bfr_lane_floats(int M) {
-  const int raw = 2 * (M * (M - 1) / 2 + M) + 4 * M;
+// Shared memory of the register kernel, per lane: the hi parts of the strict lower triangle
+// and of the c vector, the lo parts of the c vector, the lo parts of the strict lower triangle
+// (only when they are not kept in tensor memory, tm = false), one float4 of geometry per
+// neighbor (the epilogue's staging of 2 NNGP_MAX_NV + 2 (1 + NV(NV+1)/2) floats reuses the
+// front); per warp a 64-float exp table.  Blocks hold at most 8 warps and 227 KB; with tm the
+// warps per block are 4 or 8 (every lane quarter of the tensor memory in use).
+constexpr int nngp_bfr_lane_floats(int M, bool tm = false) {
+  const int nl = M * (M - 1) / 2;
+  const int raw = nl + 2 * M + (tm ? 0 : nl) + 4 * M;
   const int red = 2 * NNGP_MAX_NV + 2 * (1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2);
   return ((raw > red ? raw : red) + 3) & ~3;
 }
-constexpr size_t nngp_bfr_warp_bytes(int M) { return sizeof(float) * (32 * (size_t)nngp_bfr_lane_floats(M) + 64); }
-constexpr int nngp_bfr_max_wpb(int M) {
-  const int w = (int)((size_t)227 * 1024 / nngp_bfr_warp_bytes(M));
-  return w < 8 ? w : 8;
+constexpr size_t nngp_bfr_warp_bytes(int M, bool tm = false) {
+  return sizeof(float) * (32 * (size_t)nngp_bfr_lane_floats(M, tm) + 64);
 }
+constexpr int nngp_bfr_max_wpb(int M, bool tm = false) {
+  const int w = (int)((size_t)227 * 1024 / nngp_bfr_warp_bytes(M, tm));
+  return tm ? (w >= 8 ? 8 : (w >= 4 ? 4 : 0)) : (w < 8 ? w : 8);
+}
+// Neighbor bounds whose register kernel also comes with the lo parts in tensor memory.
+constexpr bool nngp_bfr_has_tm(int M) { return M >= 15; }
 // Writes V (n x nv row-major doubles) as float (hi, lo) pairs.
 int nngp_split_v(nngp_ctx *ctx, const double *V, int64_t count, float2 *Vf);
 

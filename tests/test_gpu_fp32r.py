@@ -76,7 +76,8 @@ def test_fp32r_matches_oracle_loglik(sp, orc):
     assert abs(loglik(ld, G, beta) - llo) <= TOL_LOGLIK * abs(llo)
 
 
-SHAPES = [(1, 0), (2, 0), (4, 0), (8, 0), (1, 1), (4, 1), (8, 2), (2, 2)]
+SHAPES = [(1, 0, 0), (2, 0, 0), (4, 0, 0), (8, 0, 0), (1, 1, 0), (4, 1, 0), (8, 2, 0), (2, 2, 0),
+          (4, 0, 1), (8, 0, 1), (4, 1, 1), (8, 2, 1)]
 
 
 @pytest.mark.parametrize("m", [10, 15, 16])
@@ -88,8 +89,8 @@ def test_launch_shape_does_not_change_results(sp, orc, m):
     ctx = sp.default_context()
     ref = None
     try:
-        for wpb, gm in SHAPES:
-            ctx.set_launch_shape(wpb, gm)
+        for wpb, gm, tm in SHAPES:
+            ctx.set_launch_shape(wpb, gm, tm)
             B, F, ld = sp.updateBF(c, o[0], o[2], m, "exponential", (1.0, 0.1, 8.0), "fp32r")
             ldg, G = sp.loglik_gram(c, o[0], o[2], m, V, "exponential", (1.0, 0.1, 8.0), "fp32r")
             got = (B, F, np.array([ld]), np.array([ldg]), G)
@@ -97,9 +98,9 @@ def test_launch_shape_does_not_change_results(sp, orc, m):
                 ref = got
             else:
                 for a, b in zip(ref, got):
-                    assert np.array_equal(a, b), (wpb, gm)
+                    assert np.array_equal(a, b), (wpb, gm, tm)
     finally:
-        ctx.set_launch_shape(0, 0)
+        ctx.set_launch_shape(0, 0, 0)
     ldt, Gt = sp.loglik_gram(c, o[0], o[2], m, V, "exponential", (1.0, 0.1, 8.0), "fp32r")
     assert ldt == ref[3][0] and np.array_equal(Gt, ref[4])
 
