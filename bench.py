@@ -130,6 +130,25 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest x over the ranks of the job (x itself for a single process): every rank
+    reports the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, max_ms: float, world_size: int) -> float:
+    """Units per second of the whole job: every rank processes units_per_rank (replicas) and
+    the job takes the slowest rank's time."""
+    return world_size * units_per_rank / (max_ms * 1e-3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -531,12 +550,8 @@ def run_ours(args):
     # FP32R headline
     ms32, kms32, launches = timed(1, args.steps, args.warmup)
     ll32 = loglik()
-    max_ms = ms32
-    if ws > 1:
-        t = torch.tensor([ms32], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        max_ms = float(t.item())
-    value = ws * N / (max_ms * 1e-3)
+    max_ms = max_over_ranks(ms32, dev)
+    value = whole_job_rate(N, max_ms, ws)
 
     # e2e: the C-ABI host entry point with pinned host buffers, copies inside the timed region
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
