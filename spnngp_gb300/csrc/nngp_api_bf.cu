@@ -93,14 +93,20 @@ struct HostIn {
   const double *V = nullptr;       // n x nv column-major
 };
 
-// Location chunks of the streamed form: about 128 K locations each (at most 8), boundaries on
-// multiples of 128 so they fall on tile boundaries of every kernel.
+// Location chunks of the streamed form: 64 K locations first, each next chunk twice the last
+// (a chunk's B/F work then takes about as long as the next chunk's copies, and the first
+// wait is short), boundaries on multiples of 128 so they fall on tile boundaries of every
+// kernel.  Inputs below 192 K locations go in one piece.
 std::vector<int> chunk_bounds(int n) {
-  int k = n / 131072;
-  k = k < 1 ? 1 : (k > 8 ? 8 : k);
   std::vector<int> b{0};
-  const int step = ((n + k - 1) / k + 127) & ~127;
-  for (int a = step; a < n; a += step) b.push_back(a);
+  if (n >= 196608) {
+    for (long step = 65536, a = 0; a + step < n;) {
+      a += step;
+      if (n - a < step / 2) break;  // fold a short tail into the last chunk
+      b.push_back((int)a);
+      step *= 2;
+    }
+  }
   b.push_back(n);
   return b;
 }
