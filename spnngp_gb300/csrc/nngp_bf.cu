@@ -40,25 +40,43 @@ __device__ double block_sum256(double x, double *sbuf) {
   return r;
 }
 
-// Fixed-order reduction of per-tile partials: block `job`, value v.  With jobs_fb, the FP64
-// re-solve's partials of the tiles marked in fb_marks are added (also in tile order).
+// Fixed-order reduction of per-tile partials: block `job`; thread t sums tiles t, t + 256, ...
+// of each value in order, then a fixed tree over the threads.  Values are taken eight at a
+// time so each thread reads whole rows of the tile-major partial array (contiguous across the
+// warp).  With jobs_fb, the FP64 re-solve's partials of the tiles marked in fb_marks are added
+// the same way (skipped when no tile was recorded: fb_count == 0).
 __global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, const BFJob *__restrict__ jobs_fb,
-                                       const unsigned *__restrict__ fb_marks, int ng,
-                                       double *__restrict__ out) {
+                                       const unsigned *__restrict__ fb_marks, const int *__restrict__ fb_count,
+                                       int ng, double *__restrict__ out) {
   const BFJob job = jobs[blockIdx.x];
   __shared__ double sbuf[256];
-  for (int v = 0; v < ng; v++) {
-    double s = 0.0;
-    for (int t = threadIdx.x; t < job.ntiles; t += 256) s += job.partial[(size_t)t * ng + v];
-    s = block_sum256(s, sbuf);
-    if (jobs_fb) {
-      const BFJob jf = jobs_fb[blockIdx.x];
-      double f = 0.0;
-      for (int t = threadIdx.x; t < jf.ntiles; t += 256)
-        if (fb_marks[jf.tile0 + t]) f += jf.partial[(size_t)t * ng + v];
-      s += block_sum256(f, sbuf);
+  const bool any_fb = jobs_fb && *fb_count > 0;
+  for (int v0 = 0; v0 < ng; v0 += 8) {
+    double acc[8], accf[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] = accf[j] = 0.0;
+    for (int t = threadIdx.x; t < job.ntiles; t += 256) {
+      const double *row = job.partial + (size_t)t * ng + v0;
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        if (v0 + j < ng) acc[j] += row[j];
     }
-    if (threadIdx.x == 0) out[(size_t)blockIdx.x * ng + v] = s;
+    if (any_fb) {
+      const BFJob jf = jobs_fb[blockIdx.x];
+      for (int t = threadIdx.x; t < jf.ntiles; t += 256) {
+        if (!fb_marks[jf.tile0 + t]) continue;
+        const double *row = jf.partial + (size_t)t * ng + v0;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          if (v0 + j < ng) accf[j] += row[j];
+      }
+    }
+#pragma unroll 1
+    for (int j = 0; j < 8 && v0 + j < ng; j++) {
+      double s = block_sum256(acc[j], sbuf);
+      if (jobs_fb) s += block_sum256(accf[j], sbuf);
+      if (threadIdx.x == 0) out[(size_t)blockIdx.x * ng + v0 + j] = s;
+    }
   }
 }
 
@@ -405,8 +423,9 @@ int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   const bool fp32r = pl->precision == NNGP_FP32R;
   // FP32R: the FP64 re-solve of the recorded tiles, folded into the same fixed-order sums
   if (fp32r && (st = launch_pass(ctx, pl, false, true, 0, 0))) return st;
-  reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr,
-                                                             fp32r ? pl->d_fb_words + 1 : nullptr, pl->ng, d_out);
+  reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(
+      pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr, fp32r ? pl->d_fb_words + 1 : nullptr,
+      fp32r ? (const int *)pl->d_fb_words : nullptr, pl->ng, d_out);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }
