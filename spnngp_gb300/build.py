@@ -1,10 +1,10 @@
 """Builds libspnngp_gb300.so in-tree from csrc/*.cu for sm_103a.
 
 Every translation unit is compiled in parallel, then linked into one shared
-library with the CUDA runtime linked statically.  nngp_bf_inst.cu and
-nngp_bfr_inst.cu are compiled once per B/F kernel variant (neighbor bound x
-precision x correlation code) so the heavy kernel instantiations spread over all
-cores.  Objects go to ``_build/`` next to the
+library with the CUDA runtime linked statically.  nngp_bf_inst.cu,
+nngp_bfr_inst.cu and nngp_bfw_inst.cu are compiled once per B/F kernel variant
+(neighbor bound x correlation code) so the heavy kernel instantiations spread
+over all cores.  Objects go to ``_build/`` next to the
 sources; the library lands next to this file.
 """
 from __future__ import annotations
@@ -27,13 +27,16 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 
 
 # source -> [(object suffix, defines)]: sources compiled once per variant
-# (FP32R with m <= 16 runs the register kernel of nngp_bfr_inst.cu, so the shared-memory
-# kernel is built in FP32R for the 24- and 32-neighbor bounds only)
+# (the shared-memory kernel of nngp_bf_inst.cu is the FP64 form; FP32R runs the register
+# kernel of nngp_bfr_inst.cu for m <= 16 and the warp-per-location kernel of nngp_bfw_inst.cu
+# for 16 < m <= 32)
 VARIANTS = {
-    "nngp_bf_inst.cu": [(f"_m{m}_{'f' if r else 'd'}_c{c}", [f"-DBF_M={m}", f"-DBF_R32={r}", f"-DBF_COV={c}"])
-                        for m, r in ((16, 0), (24, 1), (24, 0), (32, 1), (32, 0)) for c in (0, 1, 2, 3, 4)],
+    "nngp_bf_inst.cu": [(f"_m{m}_c{c}", [f"-DBF_M={m}", f"-DBF_COV={c}"])
+                        for m in (16, 24, 32) for c in (0, 1, 2, 3, 4)],
     "nngp_bfr_inst.cu": [(f"_m{m}_c{c}", [f"-DBFR_M={m}", f"-DBFR_COV={c}"])
                          for m in (10, 15, 16) for c in (0, 1, 2, 3, 4)],
+    "nngp_bfw_inst.cu": [(f"_m{m}_c{c}", [f"-DBFW_M={m}", f"-DBFW_COV={c}"])
+                         for m in (24, 32) for c in (0, 1, 2, 3, 4)],
 }
 
 
@@ -81,7 +84,7 @@ def build(verbose: bool = False, extra: list[str] | None = None, force: bool = F
     if jobs:
         workers = max(1, min(len(jobs), os.cpu_count() or 4))
         # heaviest first: the FP32R and general-model variants take longest
-        jobs.sort(key=lambda j: ("_f_" not in j[1], "_c4" not in j[1], "_m32" not in j[1], "bfr" not in j[1]))
+        jobs.sort(key=lambda j: ("bfw" not in j[1], "_c4" not in j[1], "_m32" not in j[1], "bfr" not in j[1]))
         with cf.ThreadPoolExecutor(workers) as ex:
             futs = [ex.submit(_compile, nvcc, s, o, extra + d) for s, o, d in jobs]
             for f in cf.as_completed(futs):

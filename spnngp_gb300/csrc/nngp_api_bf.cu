@@ -129,9 +129,9 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
   if (precision == NNGP_FP32R) NNGP_ALLOC(ctx, xyf, float, S_XYF, 4 * (size_t)n);
   if (mode == 1) {
     NNGP_ALLOC(ctx, Vrm, double, S_V, (size_t)n * nv);
-    // V changes from call to call under a cached plan: the register kernel's float split is
+    // V changes from call to call under a cached plan: the FP32R kernels' float split is
     // refreshed here rather than by the plan
-    if (nngp_reg_m(precision, m) > 0) NNGP_ALLOC(ctx, Vf, float2, S_VF, (size_t)n * nv);
+    if (precision == NNGP_FP32R) NNGP_ALLOC(ctx, Vf, float2, S_VF, (size_t)n * nv);
   }
   CovParams *d_theta;
   unsigned long long *d_status;

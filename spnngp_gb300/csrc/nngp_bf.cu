@@ -5,17 +5,18 @@
 #include "nngp_internal.h"
 
 // Host side of the B/F pass: plans (job tables), dispatch to the kernel
-// instantiations (nngp_bf_inst.cu: the shared-memory kernels, one object per
-// neighbor bound, precision and correlation code; nngp_bfr_inst.cu: the
-// register FP32R kernel for m <= 16), the autotuner of the register kernel's
-// launch shape, and the fixed-order reductions.  The kernels are documented in
-// nngp_bf_kernel.cuh and nngp_bfr_kernel.cuh.
+// instantiations (nngp_bf_inst.cu: the FP64 shared-memory kernel, one object per
+// neighbor bound and correlation code; nngp_bfr_inst.cu: the register FP32R
+// kernel for m <= 16; nngp_bfw_inst.cu: the warp-per-location FP32R kernel for
+// 16 < m <= 32), the autotuner of the register kernel's launch shape, and the
+// fixed-order reductions.  The kernels are documented in nngp_bf_kernel.cuh,
+// nngp_bfr_kernel.cuh and nngp_bfw_kernel.cuh.
 namespace nngp_bf {
-template <int M, bool R32, int MODE, int COV>
+template <int M, int MODE, int COV>
 int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
-template <int M, bool R32>
+template <int M>
 constexpr int bf_tpb() {
-  return R32 ? (M <= 16 ? 128 : 64) : (M <= 16 ? 64 : 32);
+  return M <= 16 ? 64 : 32;
 }
 }  // namespace nngp_bf
 namespace nngp_bfr {
@@ -24,6 +25,10 @@ int launch_reg(nngp_ctx *ctx, const BFPlan *pl, int wpb, int grid, int t0, int t
 template <int M, int MODE, int COV>
 int occupancy(int wpb, int tm);
 }  // namespace nngp_bfr
+namespace nngp_bfw {
+template <int M, int MODE, int COV>
+int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1);
+}  // namespace nngp_bfw
 using namespace nngp_bf;
 
 namespace {
@@ -83,27 +88,42 @@ __global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, const BFJ
 }  // namespace
 
 namespace {
+// The FP64 kernel: the FP64 form's primary pass, or the re-solve of the locations an FP32R
+// pass flagged (fallback_pass)
 template <int MODE, int COV>
-int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
-  // FP32R with m <= 16 runs the register kernel (launched by run_reg); the FP64
-  // re-solve of its flagged locations lands here with fp32r false
-  if (pl->mmax <= 16) return launch_one<16, false, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
-  if (pl->mmax <= 24)
-    return fp32r ? launch_one<24, true, MODE, COV>(ctx, pl, fallback_pass, t0, t1)
-                 : launch_one<24, false, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
-  return fp32r ? launch_one<32, true, MODE, COV>(ctx, pl, fallback_pass, t0, t1)
-               : launch_one<32, false, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1) {
+  if (pl->mmax <= 16) return launch_one<16, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  if (pl->mmax <= 24) return launch_one<24, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  return launch_one<32, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
 }
 
 template <int MODE>
-int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
+int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1) {
   switch (pl->cov) {
-    case NNGP_COV_EXP: return launch_mode_c<MODE, NNGP_COV_EXP>(ctx, pl, fp32r, fallback_pass, t0, t1);
-    case NNGP_COV_SPH: return launch_mode_c<MODE, NNGP_COV_SPH>(ctx, pl, fp32r, fallback_pass, t0, t1);
-    case NNGP_COV_MAT_HALF: return launch_mode_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, fp32r, fallback_pass, t0, t1);
-    case NNGP_COV_GAU: return launch_mode_c<MODE, NNGP_COV_GAU>(ctx, pl, fp32r, fallback_pass, t0, t1);
-    default: return launch_mode_c<MODE, NNGP_COV_ANY>(ctx, pl, fp32r, fallback_pass, t0, t1);
+    case NNGP_COV_EXP: return launch_mode_c<MODE, NNGP_COV_EXP>(ctx, pl, fallback_pass, t0, t1);
+    case NNGP_COV_SPH: return launch_mode_c<MODE, NNGP_COV_SPH>(ctx, pl, fallback_pass, t0, t1);
+    case NNGP_COV_MAT_HALF: return launch_mode_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, fallback_pass, t0, t1);
+    case NNGP_COV_GAU: return launch_mode_c<MODE, NNGP_COV_GAU>(ctx, pl, fallback_pass, t0, t1);
+    default: return launch_mode_c<MODE, NNGP_COV_ANY>(ctx, pl, fallback_pass, t0, t1);
   }
+}
+
+// The warp-per-location FP32R kernel (16 < m <= 32) on tiles [t0, t1)
+template <int M, int MODE>
+int warp_call_m(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  using namespace nngp_bfw;
+  switch (pl->cov) {
+    case NNGP_COV_EXP: return launch_warp<M, MODE, NNGP_COV_EXP>(ctx, pl, t0, t1);
+    case NNGP_COV_SPH: return launch_warp<M, MODE, NNGP_COV_SPH>(ctx, pl, t0, t1);
+    case NNGP_COV_MAT_HALF: return launch_warp<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, t0, t1);
+    case NNGP_COV_GAU: return launch_warp<M, MODE, NNGP_COV_GAU>(ctx, pl, t0, t1);
+    default: return launch_warp<M, MODE, NNGP_COV_ANY>(ctx, pl, t0, t1);
+  }
+}
+int warp_call(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  const bool m1 = pl->mode == 1;
+  if (pl->mmax <= 24) return m1 ? warp_call_m<24, 1>(ctx, pl, t0, t1) : warp_call_m<24, 0>(ctx, pl, t0, t1);
+  return m1 ? warp_call_m<32, 1>(ctx, pl, t0, t1) : warp_call_m<32, 0>(ctx, pl, t0, t1);
 }
 
 // ---------------------------------------------------------------- register kernel
@@ -259,17 +279,16 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
 
 // Primary pass over tiles [t0, t1), or (fallback_pass) the FP64 re-solve of the recorded tiles.
 int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
-  if (fp32r && !fallback_pass && pl->reg_m > 0) return run_reg(ctx, pl, t0, t1);
-  return pl->mode == 0 ? launch_mode<0>(ctx, pl, fp32r, fallback_pass, t0, t1)
-                       : launch_mode<1>(ctx, pl, fp32r, fallback_pass, t0, t1);
+  if (fp32r && !fallback_pass) return pl->reg_m > 0 ? run_reg(ctx, pl, t0, t1) : warp_call(ctx, pl, t0, t1);
+  return pl->mode == 0 ? launch_mode<0>(ctx, pl, fallback_pass, t0, t1)
+                       : launch_mode<1>(ctx, pl, fallback_pass, t0, t1);
 }
 
 }  // namespace
 
 int nngp_bf_tile(int precision, int mmax) {
-  if (nngp_reg_m(precision, mmax) > 0) return 32;  // the register kernel's tiles are warps
-  if (precision == NNGP_FP32R) return bf_tpb<32, true>();
-  return mmax <= 16 ? bf_tpb<16, false>() : bf_tpb<32, false>();
+  if (precision == NNGP_FP32R) return 32;  // both FP32R kernels' tiles are one warp's
+  return mmax <= 16 ? bf_tpb<16>() : bf_tpb<32>();
 }
 
 void *nngp_malloc_async(nngp_ctx *ctx, size_t bytes) {
@@ -355,10 +374,10 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
       jobs[k].fb_list = pl->d_fb_list;
     }
   }
-  // the register kernel reads V as float (hi, lo) pairs: split it once for callers that
-  // did not provide them (their V stays fixed for the plan's lifetime)
+  // the FP32R kernels read V as float (hi, lo) pairs: split it once for callers that did not
+  // provide them (their V stays fixed for the plan's lifetime)
   std::vector<BFData> dv(datas);
-  if (pl->reg_m > 0 && mode == 1) {
+  if (precision == NNGP_FP32R && mode == 1) {
     for (BFData &d : dv) {
       if (d.Vf || !d.V) continue;
       float2 *vf = (float2 *)own(sizeof(float2) * (size_t)d.n * nv);

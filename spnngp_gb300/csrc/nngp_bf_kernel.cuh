@@ -12,17 +12,10 @@
 // shared load per FMA.  The forward solve for c is fused into the factor loop;
 // B is the back substitution.
 //
-// Precision modes:
-//   FP64   everything in double.
-//   FP32R  (built for the 32-neighbor bound; m <= 16 runs the register kernel of
-//          nngp_bfr_kernel.cuh) coordinates split into float hi/lo parts and
-//          differenced exactly; covariance build, Cholesky and both triangular
-//          solves in float; then one refinement step: the residual c - C b of the
-//          float-evaluated C accumulated as a compensated (Dot2) float pair, the
-//          correction solved with the float factor, B = b + delta kept in FP64.
-//          F, log F and the Gram sums are FP64.  A location whose float pivot is
-//          not positive, or whose F is below 1e-3 (sigma^2 + tau^2), is flagged and
-//          re-solved by the FP64 kernel, which walks the list of flagged tiles.
+// This is the FP64 form (everything in double), and the FP64 re-solve of the
+// locations the FP32R kernels flag (nngp_bfr_kernel.cuh for m <= 16,
+// nngp_bfw_kernel.cuh for 16 < m <= 32): that pass walks the list of flagged
+// tiles and solves only the flagged locations.
 //
 // Modes: 0 writes B (packed, nIndx) and F and per-tile sums of log F;
 //        1 (fused likelihood) writes no B/F but per-tile sums of log F and of
@@ -31,15 +24,12 @@
 // launch shape or on block scheduling.
 #pragma once
 #include <cuda_runtime.h>
-#include <type_traits>
 #include "nngp_internal.h"
 #include "nngp_math.cuh"
 
 namespace nngp_bf {
 
 constexpr int kNGMax = 1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2;
-// FP32R hands a location to the FP64 kernel when F < kFp32rMinF * (sigma^2 + tau^2).
-constexpr double kFp32rMinF = 1e-3;
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -67,33 +57,6 @@ template <int M>
 __host__ __device__ constexpr int tri_size() { return M * (M + 1) / 2; }
 __host__ __device__ constexpr int tri_at(int r, int c) { return r * (r + 1) / 2 + c; }
 
-// Error-free transformations on the FP32 pipe (Knuth's TwoSum; TwoProduct by FMA),
-// as used by Ogita, Rump & Oishi's compensated dot product (Dot2, SIAM J. Sci.
-// Comput. 26, 2005): the refinement residual is accumulated as a float pair that
-// carries about twice float precision.  The _rn intrinsics keep the compiler from
-// contracting or reassociating them.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = __fadd_rn(a, b);
-  const float bv = __fsub_rn(s, a);
-  const float av = __fsub_rn(s, bv);
-  e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
-}
-// (s, e) with s + e = a - b exactly.
-__device__ __forceinline__ void two_diff(float a, float b, float &s, float &e) {
-  s = __fsub_rn(a, b);
-  const float bv = __fsub_rn(s, a);
-  const float av = __fsub_rn(s, bv);
-  e = __fsub_rn(__fsub_rn(a, av), __fadd_rn(b, bv));
-}
-// acc_hi + acc_lo += x * y with the product's rounding error carried.
-__device__ __forceinline__ void dot2_acc(float &hi, float &lo, float x, float y) {
-  const float p = __fmul_rn(x, y);
-  const float pe = __fmaf_rn(x, y, -p);
-  float q;
-  two_sum(hi, p, hi, q);
-  lo = __fadd_rn(lo, __fadd_rn(q, pe));
-}
-
 // v[k] for a runtime k < NNGP_MAX_NV without indexing a local array
 __device__ __forceinline__ double pick_nv(const double (&v)[NNGP_MAX_NV], int k) {
   double r = 0.0;
@@ -104,7 +67,7 @@ __device__ __forceinline__ double pick_nv(const double (&v)[NNGP_MAX_NV], int k)
 }
 
 // --------------------------------------------------------------------- kernel
-template <int M, bool R32, int MODE, int TPB, int COV>
+template <int M, int MODE, int TPB, int COV>
 __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ datas,
                                                  const CovParams *__restrict__ thetas,
                                                  const BFJob *__restrict__ jobs, int njobs,
@@ -112,19 +75,15 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
                                                  unsigned long long *__restrict__ status,
                                                  int only_flagged, const int *__restrict__ tile_list,
                                                  const int *__restrict__ tile_count) {
-  using T = typename std::conditional<R32, float, double>::type;
   constexpr int TRI = tri_size<M>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *tri = reinterpret_cast<T *>(smem_raw);
-  // per-neighbor geometry: FP32R 4 floats (dx hi, dy hi, dx lo, dy lo) relative to the
-  // location; FP64 2 doubles (absolute x, y)
-  T *geo = tri + (size_t)TRI * TPB;
-  constexpr int GEO = R32 ? 4 : 2;
-  double *wbuf = reinterpret_cast<double *>(geo + (size_t)GEO * M * TPB);
+  double *tri = reinterpret_cast<double *>(smem_raw);
+  double *geo = tri + (size_t)TRI * TPB;  // per-neighbor absolute (x, y)
+  double *wbuf = geo + (size_t)2 * M * TPB;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
 #define TRI_(r, c) tri[(size_t)tri_at((r), (c)) * TPB + tid]
-#define GEO_(k, q) geo[(size_t)((k) * GEO + (q)) * TPB + tid]
+#define GEO_(k, q) geo[(size_t)((k) * 2 + (q)) * TPB + tid]
 
   // the FP64 re-solve walks the list of tiles the FP32R pass recorded; the other passes walk
   // tiles [tile_begin, tile_end)
@@ -154,113 +113,72 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
       off = d.nnLU[i];
       mi = d.nnLU[d.n + i];
     }
-    if constexpr (R32) {
-      // coordinates arrive split as float (hi, lo) pairs; differences stay exact to ~2^-48
-      const float4 pi4 = active ? reinterpret_cast<const float4 *>(d.xyf)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < M; k++) {
-        nb[k] = 0;
-        if (k < mi) {
-          nb[k] = d.nnIndx[off + k];
-          const float4 q = reinterpret_cast<const float4 *>(d.xyf)[nb[k]];
-          float hx, lx, hy, ly;
-          two_diff(q.x, pi4.x, hx, lx);
-          two_diff(q.y, pi4.y, hy, ly);
-          GEO_(k, 0) = hx;
-          GEO_(k, 1) = hy;
-          GEO_(k, 2) = __fadd_rn(lx, __fsub_rn(q.z, pi4.z));
-          GEO_(k, 3) = __fadd_rn(ly, __fsub_rn(q.w, pi4.w));
-        }
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < M; k++) {
-        nb[k] = 0;
-        if (k < mi) {
-          nb[k] = d.nnIndx[off + k];
-          const double2 q = reinterpret_cast<const double2 *>(d.xy)[nb[k]];
-          GEO_(k, 0) = q.x;
-          GEO_(k, 1) = q.y;
-        }
+    for (int k = 0; k < M; k++) {
+      nb[k] = 0;
+      if (k < mi) {
+        nb[k] = d.nnIndx[off + k];
+        const double2 q = reinterpret_cast<const double2 *>(d.xy)[nb[k]];
+        GEO_(k, 0) = q.x;
+        GEO_(k, 1) = q.y;
       }
     }
 
     // ---- covariance build: c (registers) and the lower triangle of C (shared)
-    T cv[M];
-    const T s2 = (T)sigmaSq, t2 = (T)tauSq;
-    const float phif = (float)cpp->phi;
+    double cv[M];
     double xi = 0.0, yi = 0.0;
-    if constexpr (!R32) {
-      if (active) {
-        const double2 p = reinterpret_cast<const double2 *>(d.xy)[i];
-        xi = p.x;
-        yi = p.y;
-      }
+    if (active) {
+      const double2 p = reinterpret_cast<const double2 *>(d.xy)[i];
+      xi = p.x;
+      yi = p.y;
     }
 #pragma unroll
     for (int r = 0; r < M; r++) {
-      cv[r] = (T)0;
+      cv[r] = 0.0;
       if (r < mi) {
-        if constexpr (R32) {
-          const float hx = GEO_(r, 0), hy = GEO_(r, 1);
-          cv[r] = s2 * nngp_cor_f<COV>(hx * hx + hy * hy, *cpp, phif);
+        const double xr = GEO_(r, 0), yr = GEO_(r, 1);
+        const double ax = xi - xr, ay = yi - yr;
+        cv[r] = sigmaSq * nngp_cor_d<COV>(sqrt(ax * ax + ay * ay), *cpp);
 #pragma unroll
-          for (int c = 0; c <= r; c++) {
-            float e;
-            if (c == r) {
-              e = s2 + t2;  // every model has rho(0) = 1
-            } else {
-              const float ex = (GEO_(r, 0) - GEO_(c, 0)) + (GEO_(r, 2) - GEO_(c, 2));
-              const float ey = (GEO_(r, 1) - GEO_(c, 1)) + (GEO_(r, 3) - GEO_(c, 3));
-              e = s2 * nngp_cor_f<COV>(ex * ex + ey * ey, *cpp, phif);
-            }
-            TRI_(r, c) = (T)e;
-          }
-        } else {
-          const double xr = GEO_(r, 0), yr = GEO_(r, 1);
-          const double ax = xi - xr, ay = yi - yr;
-          cv[r] = sigmaSq * nngp_cor_d<COV>(sqrt(ax * ax + ay * ay), *cpp);
-#pragma unroll
-          for (int c = 0; c <= r; c++) {
-            const double bx = xr - GEO_(c, 0), by = yr - GEO_(c, 1);
-            double e = sigmaSq * nngp_cor_d<COV>(sqrt(bx * bx + by * by), *cpp);
-            if (c == r) e += tauSq;
-            TRI_(r, c) = (T)e;
-          }
+        for (int c = 0; c <= r; c++) {
+          const double bx = xr - GEO_(c, 0), by = yr - GEO_(c, 1);
+          double e = sigmaSq * nngp_cor_d<COV>(sqrt(bx * bx + by * by), *cpp);
+          if (c == r) e += tauSq;
+          TRI_(r, c) = e;
         }
       }
     }
 
     // ---- Cholesky (row-oriented) fused with the forward solve L z = c; two partial sums per
     // inner product shorten the dependency chains
-    T invd[M], z[M];
+    double invd[M], z[M];
     bool ok = true;
 #pragma unroll
     for (int r = 0; r < M; r++) {
-      invd[r] = (T)0;
-      z[r] = (T)0;
+      invd[r] = 0.0;
+      z[r] = 0.0;
       if (r < mi) {
-        T row[M];
+        double row[M];
 #pragma unroll
         for (int c = 0; c <= r; c++) {
-          T s0 = TRI_(r, c), s1 = (T)0;
+          double s0 = TRI_(r, c), s1 = 0.0;
 #pragma unroll
           for (int k = 0; k < c; k++) {
-            const T l = (c == r) ? row[k] : TRI_(c, k);
+            const double l = (c == r) ? row[k] : TRI_(c, k);
             if (k & 1) s1 -= row[k] * l;
             else s0 -= row[k] * l;
           }
-          const T s = s0 + s1;
+          const double s = s0 + s1;
           if (c < r) {
             row[c] = s * invd[c];
           } else {
-            ok = ok && (s > (T)0);
-            const T dg = sqrt(s);
+            ok = ok && (s > 0.0);
+            const double dg = sqrt(s);
             row[r] = dg;
-            invd[r] = (T)1 / dg;
+            invd[r] = 1.0 / dg;
           }
         }
-        T zs0 = cv[r], zs1 = (T)0;
+        double zs0 = cv[r], zs1 = 0.0;
 #pragma unroll
         for (int k = 0; k < r; k++) {
           if (k & 1) zs1 -= row[k] * z[k];
@@ -272,96 +190,27 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
       }
     }
 
-    // ---- back substitution L' b = z
-    T bb[M];
+    // ---- back substitution L' B = z
+    double Bd[M];
 #pragma unroll
     for (int k = M - 1; k >= 0; k--) {
-      bb[k] = (T)0;
+      Bd[k] = 0.0;
       if (k < mi) {
-        bb[k] = z[k] * invd[k];
+        Bd[k] = z[k] * invd[k];
 #pragma unroll
-        for (int r = 0; r < k; r++) z[r] -= TRI_(k, r) * bb[k];
+        for (int r = 0; r < k; r++) z[r] -= TRI_(k, r) * Bd[k];
       }
     }
+    if (!ok && active) record_status(status, 1, i);
 
-    double Bd[M];
-    if constexpr (R32) {
-      if (!ok && active) {
-        // float pivot failed: leave this location to the FP64 kernel
-        nngp_flag_for_fp64(job, i);
-        active = false;
-        mi = 0;
-      }
-      // ---- refinement residual res = c - C b, accumulated as a float pair (Dot2) with C rebuilt
-      float sh[M], sl[M];
-#pragma unroll
-      for (int r = 0; r < M; r++) {
-        sh[r] = 0.f;
-        sl[r] = 0.f;
-      }
-#pragma unroll
-      for (int r = 0; r < M; r++) {
-        if (r < mi) {
-#pragma unroll
-          for (int c = 0; c <= r; c++) {
-            float e;
-            if (c == r) {
-              e = s2 + t2;
-            } else {
-              const float ex = (GEO_(r, 0) - GEO_(c, 0)) + (GEO_(r, 2) - GEO_(c, 2));
-              const float ey = (GEO_(r, 1) - GEO_(c, 1)) + (GEO_(r, 3) - GEO_(c, 3));
-              e = s2 * nngp_cor_f<COV>(ex * ex + ey * ey, *cpp, phif);
-            }
-            dot2_acc(sh[r], sl[r], e, bb[c]);
-            if (c < r) dot2_acc(sh[c], sl[c], e, bb[r]);
-          }
-        }
-      }
-      // correction: L L' delta = res, in float with the float factor
-      T w[M];
-#pragma unroll
-      for (int r = 0; r < M; r++) {
-        w[r] = (T)0;
-        if (r < mi) {
-          T s = __fsub_rn(__fsub_rn(cv[r], sh[r]), sl[r]);
-#pragma unroll
-          for (int k = 0; k < r; k++) s -= TRI_(r, k) * w[k];
-          w[r] = s * invd[r];
-        }
-      }
-#pragma unroll
-      for (int k = M - 1; k >= 0; k--) {
-        Bd[k] = 0.0;
-        if (k < mi) {
-          const T dk = w[k] * invd[k];
-#pragma unroll
-          for (int r = 0; r < k; r++) w[r] -= TRI_(k, r) * dk;
-          Bd[k] = (double)bb[k] + (double)dk;
-        }
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < M; k++) Bd[k] = (double)bb[k];
-      if (!ok && active) record_status(status, 1, i);
-    }
-
-    // ---- F = sigma^2 + tau^2 - B'c in FP64
+    // ---- F = sigma^2 + tau^2 - B'c
     double Fi;
     {
       double dot = 0.0;
 #pragma unroll
       for (int k = 0; k < M; k++)
-        if (k < mi) dot = fma(Bd[k], (double)cv[k], dot);
+        if (k < mi) dot = fma(Bd[k], cv[k], dot);
       Fi = sigmaSq - dot + tauSq;
-    }
-    if constexpr (R32) {
-      // a conditional variance this small is dominated by the float rounding of C:
-      // hand the location to the FP64 kernel
-      if (active && !(Fi > kFp32rMinF * (sigmaSq + tauSq))) {
-        nngp_flag_for_fp64(job, i);
-        active = false;
-        mi = 0;
-      }
     }
     const double logF = active ? log(Fi) : 0.0;
 
@@ -426,19 +275,17 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
 #undef GEO_
 }
 
-template <int M, bool R32>
+template <int M>
 constexpr int bf_tpb() {
-  return R32 ? (M <= 16 ? 128 : 64) : (M <= 16 ? 64 : 32);
+  return M <= 16 ? 64 : 32;
 }
 
-template <int M, bool R32, int MODE, int COV>
+template <int M, int MODE, int COV>
 int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1) {
-  constexpr int TPB = bf_tpb<M, R32>();
-  using T = typename std::conditional<R32, float, double>::type;
-  constexpr int GEO = R32 ? 4 : 2;
-  const size_t smem = sizeof(T) * ((size_t)tri_size<M>() + (size_t)GEO * M) * TPB +
+  constexpr int TPB = bf_tpb<M>();
+  const size_t smem = sizeof(double) * ((size_t)tri_size<M>() + (size_t)2 * M) * TPB +
                       sizeof(double) * (TPB / 32) * kNGMax;
-  auto kern = bf_kernel<M, R32, MODE, TPB, COV>;
+  auto kern = bf_kernel<M, MODE, TPB, COV>;
   static bool configured = false;  // once per instantiation
   if (!configured) {
     NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -1,0 +1,375 @@
+// FP32R B/F kernel for neighbor bounds 16 < m <= 32 (M = 24, 32): one warp per location
+// (reference updateBF, src/rNNGP.cpp:46-101; updateConjBF, src/cNNGP.cpp:24-69; the
+// likelihood sums of src/rNNGP.cpp:306-317 and Q, src/util.cpp:261-280).
+//
+// A 32-neighbor factor (528 entries) does not fit one thread's registers, so lane r of a warp
+// owns row r of the neighborhood system.  A warp walks a tile of 32 consecutive locations of
+// one job (job = one dataset at one parameter set), one location at a time:
+//   1. geometry: lane k differences neighbor k from the location (float hi/lo coordinate
+//      splits, as normalised double-float pairs); the largest offset of the location fixes a
+//      common grid 2^e for the hi parts, so two hi parts subtract exactly; the quantised
+//      offsets go to the warp's shared memory, one float4 per neighbor;
+//   2. covariance in double-float (the arithmetic of the m <= 16 kernel, nngp_cov_df.cuh):
+//      lane k evaluates c_k; the pairs of the strict lower triangle are spread evenly over the
+//      lanes (pair e on lane e % 32) and stored, hi and lo parts, in the warp's triangle;
+//   3. right-looking Cholesky of the hi parts with lane r holding row r in registers: step k
+//      broadcasts the pivot and column k by shuffles (a broadcast through shared memory
+//      would take fewer instructions, but the compiler then schedules its loads into more
+//      than 255 live registers); L then goes to shared memory so that the back
+//      substitution can read its columns;
+//   4. forward and back substitution in float, one shuffle per step (lane k sends its
+//      component times its own 1 / L_kk);
+//   5. one refinement step: lane r forms res_r = c_r - sum_c C[r][c] b_c over the
+//      double-float entries (a compensated Dot2 sum), and the correction delta is solved with
+//      the float factor; B = b + delta as an unevaluated float pair;
+//   6. F = sigma^2 + tau^2 - B'c (a double-float warp sum), the error estimate of the m <= 16
+//      kernel -- a location is flagged and left to the FP64 kernel when its float pivot fails,
+//      when q^2 (sigma^2 + tau^2) > 1e-8 F (q = |delta|_inf / |b|_inf) or when
+//      F < 1e-6 (sigma^2 + tau^2) --, log F, and in the fused pass r = (I - B) V and
+//      r_a r_b / F.  Lane t adds value t of each location to its running double-float sum in
+//      location order, so a tile's sums have a fixed order whatever the launch shape.
+// Rows m_i <= r < 32 are the identity (c_r = 0, B_r = 0), so every step runs on all lanes.
+#pragma once
+#include <cuda_runtime.h>
+#include "nngp_cov_df.cuh"
+
+namespace nngp_bfw {
+
+using nngp_bfr::CorDF;
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Per-warp shared memory (floats): the geometry (32 float4), the hi and lo parts of C's strict
+// lower triangle and the float factor's strict lower triangle (row-major, (r, c) at
+// r (r - 1) / 2 + c), the exp table (32 hi, 32 lo), the float solution b and the fused pass's
+// residuals r_v (hi, lo).
+template <int M>
+struct WShape {
+  static constexpr int NL = M * (M - 1) / 2;
+  static constexpr int NLP = (NL + 3) & ~3;
+  static constexpr int GEO = 0;
+  static constexpr int CH = GEO + 4 * 32;
+  static constexpr int CL = CH + NLP;
+  static constexpr int LT = CL + NLP;
+  static constexpr int TAB = LT + NLP;
+  static constexpr int BV = TAB + 64;
+  static constexpr int RV = BV + 32;
+  static constexpr int WARP_FLOATS = (RV + 2 * NNGP_MAX_NV + 3) & ~3;
+};
+
+__device__ __forceinline__ constexpr int tri(int r) { return r * (r - 1) / 2; }
+
+// (r, c) of strict-lower-triangle entry e (e = tri(r) + c, c < r)
+__device__ __forceinline__ void pair_of(int e, int &r, int &c) {
+  r = (int)((1.0f + sqrtf((float)(8 * e + 1))) * 0.5f);
+  c = e - tri(r);
+  if (c < 0) {
+    r--;
+    c += r;
+  } else if (c >= r) {
+    c -= r;
+    r++;
+  }
+}
+
+// Sum over the warp of a double-float value (butterfly; the double-float add is commutative,
+// so every lane ends with the same sum)
+__device__ __forceinline__ nngp_df::df warp_sum_df(nngp_df::df p) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const nngp_df::df q{__shfl_xor_sync(kFull, p.h, o), __shfl_xor_sync(kFull, p.l, o)};
+    p = nngp_df::add(p, q);
+  }
+  return p;
+}
+
+// (b + delta)(x + xl) as a double-float (the delta * xl term is below the pair's precision)
+__device__ __forceinline__ nngp_df::df prod_df(float b, float delta, float x, float xl) {
+  const float ph = __fmul_rn(b, x);
+  const float pe = __fmaf_rn(b, x, -ph);
+  return nngp_df::norm(ph, __fmaf_rn(delta, x, __fmaf_rn(b, xl, pe)));
+}
+
+template <int M, int MODE, int COV>
+__global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ datas,
+                                                  const CovParams *__restrict__ thetas,
+                                                  const BFJob *__restrict__ jobs, int njobs, int tile_begin,
+                                                  int tile_end, int nv) {
+  namespace F = nngp_df;
+  namespace G = nngp_df2;
+  using S = WShape<M>;
+  extern __shared__ __align__(16) float smem_w[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  float *ws = smem_w + (size_t)warp * S::WARP_FLOATS;
+  float4 *geo = reinterpret_cast<float4 *>(ws + S::GEO);
+  float *chs = ws + S::CH, *cls = ws + S::CL, *lts = ws + S::LT, *tab = ws + S::TAB;
+  float *bvs = ws + S::BV, *rvs = ws + S::RV;
+  const int ng = MODE == 0 ? 1 : 1 + nv * (nv + 1) / 2;
+  const int tl = tri(lane);  // this lane's row start in the triangles
+  const bool row_lane = lane < M;
+
+  for (int kt = blockIdx.x * wpb + warp; kt < tile_end - tile_begin; kt += gridDim.x * wpb) {
+    const int tile = tile_begin + kt;
+    const BFJob job = jobs[nngp_bfr::find_job(jobs, njobs, tile)];
+    const BFData d = datas[job.data];
+    const CovParams *cpp = thetas + job.theta;
+    const int tj = tile - job.tile0;
+    const CorDF ck = nngp_bfr::cor_prepare<COV>(cpp);
+    const F::df Sd{cpp->dfDiag[0], cpp->dfDiag[1]};  // the diagonal sigma^2 + tau^2
+    {  // the warp's exp table: sigma^2 2^(j/32)
+      const float2 t2 = F::kExp2Tab[lane];
+      const F::df e = F::mul(ck.S2, F::df{t2.x, t2.y});
+      tab[lane] = e.h;
+      tab[32 + lane] = e.l;
+    }
+    __syncwarp();
+    F::df acc0{0.0f, 0.0f}, acc1{0.0f, 0.0f};
+    const int i_end = min(d.n, (tj + 1) * 32);
+    const float4 *xyf = reinterpret_cast<const float4 *>(d.xyf);
+
+#pragma unroll 1
+    for (int i = tj * 32; i < i_end; i++) {
+      const int off = d.nnLU[i];
+      const int mi = min(d.nnLU[d.n + i], M);
+      const bool pad = lane >= mi;  // identity row
+
+      // ---- 1. geometry
+      const float4 pi4 = xyf[i];
+      F::df ox{0.0f, 0.0f}, oy{0.0f, 0.0f};
+      int nbk = 0;
+      if (!pad) {
+        nbk = d.nnIndx[off + lane];
+        const float4 q = xyf[nbk];
+        ox = F::diff(q.x, q.z, pi4.x, pi4.z);
+        oy = F::diff(q.y, q.w, pi4.y, pi4.w);
+      }
+      // largest |offset| hi part (non-negative floats order as their bit patterns)
+      const float omax = fmaxf(1e-30f, __int_as_float((int)__reduce_max_sync(
+                                           kFull, (unsigned)__float_as_int(fmaxf(fabsf(ox.h), fabsf(oy.h))))));
+      float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      {
+        const int eb = ((__float_as_int(omax) >> 23) & 0xff) - 22;  // biased exponent of 2^e
+        const float grid = __int_as_float(max(eb, 1) << 23), inv = __int_as_float((254 - max(eb, 1)) << 23);
+        if (!pad) {
+          const float hx = __fmul_rn(rintf(__fmul_rn(ox.h, inv)), grid);
+          const float hy = __fmul_rn(rintf(__fmul_rn(oy.h, inv)), grid);
+          g = make_float4(hx, hy, __fadd_rn(__fsub_rn(ox.h, hx), ox.l), __fadd_rn(__fsub_rn(oy.h, hy), oy.l));
+        }
+      }
+      geo[lane] = g;
+
+      // ---- 2. covariance: c_k on lane k, then the strict lower triangle spread over the lanes
+      F::df cv{0.0f, 0.0f};
+      if (!pad) {
+        const F::df gx = F::norm(g.x, g.z), gy = F::norm(g.y, g.w);
+        cv = nngp_bfr::cov_df<COV>(F::sumsq(gx.h, gx.l, gy.h, gy.l), ck, tab, cpp);
+      }
+      __syncwarp();
+      constexpr int NIT = (S::NL + 31) / 32;
+#pragma unroll 1
+      for (int t = 0; t < NIT; t += 2) {
+        int e[2], r[2], c[2];
+        float4 gr[2], gc[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+          e[u] = lane + 32 * (t + u);
+          pair_of(min(e[u], S::NL - 1), r[u], c[u]);
+          gr[u] = geo[r[u]];
+          gc[u] = geo[c[u]];
+        }
+        F::df v[2];
+        if constexpr (nngp_bfr::kPacked<COV>) {
+          // hi parts on the common grid: their difference is exact
+          G::df2 ex, ey;
+          G::fast_two_sum(G::sub(G::pack(gr[0].x, gr[1].x), G::pack(gc[0].x, gc[1].x)),
+                          G::sub(G::pack(gr[0].z, gr[1].z), G::pack(gc[0].z, gc[1].z)), ex.h, ex.l);
+          G::fast_two_sum(G::sub(G::pack(gr[0].y, gr[1].y), G::pack(gc[0].y, gc[1].y)),
+                          G::sub(G::pack(gr[0].w, gr[1].w), G::pack(gc[0].w, gc[1].w)), ey.h, ey.l);
+          const G::df2 rr = nngp_bfr::cov_df2<COV>(G::sumsq(ex, ey), ck, tab);
+          v[0] = F::df{G::first(rr.h), G::first(rr.l)};
+          v[1] = F::df{G::second(rr.h), G::second(rr.l)};
+        } else {
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            F::df ex, ey;
+            F::fast_two_sum(__fsub_rn(gr[u].x, gc[u].x), __fsub_rn(gr[u].z, gc[u].z), ex.h, ex.l);
+            F::fast_two_sum(__fsub_rn(gr[u].y, gc[u].y), __fsub_rn(gr[u].w, gc[u].w), ey.h, ey.l);
+            v[u] = nngp_bfr::cov_df<COV>(F::sumsq(ex.h, ex.l, ey.h, ey.l), ck, tab, cpp);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+          if (e[u] < S::NL) {
+            const bool live = r[u] < mi;  // rows past m_i are the identity's
+            chs[e[u]] = live ? v[u].h : 0.0f;
+            cls[e[u]] = live ? v[u].l : 0.0f;
+          }
+        }
+      }
+      __syncwarp();
+
+      // ---- 3. Cholesky of the hi parts: lane r holds row r (entries c <= r are meaningful)
+      float row[M];
+#pragma unroll
+      for (int c = 0; c < M; c++) {
+        if (c == lane) row[c] = pad ? 1.0f : Sd.h;
+        else row[c] = (c < lane && row_lane) ? chs[tl + c] : 0.0f;
+      }
+      bool ok = true;
+      float ivmine = 1.0f;  // 1 / L_rr on lane r
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float dk = __shfl_sync(kFull, row[k], k);
+        ok = ok && (dk > 0.0f);
+        const float ik = rsqrtf(dk);
+        if (lane == k) ivmine = ik;
+        const float lk = __fmul_rn(row[k], ik);  // L[r][k] on lane r > k
+        row[k] = lk;
+        if (k + 1 < M) {
+#pragma unroll
+          for (int j = k + 1; j < M; j++) row[j] = fmaf(-lk, __shfl_sync(kFull, lk, j), row[j]);
+        }
+      }
+      // L to shared memory for the column reads of the back substitution
+#pragma unroll
+      for (int c = 0; c < M - 1; c++)
+        if (c < lane && row_lane) lts[tl + c] = row[c];
+      __syncwarp();
+
+      // ---- 4. L z = c, L' b = z (lane r holds component r; every lane keeps b)
+      // step k: lane k's component times its 1 / L_kk, broadcast
+      float t = cv.h;
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float zk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
+        t = lane > k ? fmaf(-row[k], zk, t) : (lane == k ? zk : t);
+      }
+      float bmine = 0.0f, bmax = 0.0f;
+#pragma unroll 4
+      for (int k = M - 1; k >= 0; k--) {
+        const float bk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
+        bmax = fmaxf(bmax, fabsf(bk));
+        if (lane == k) {
+          bmine = bk;
+          bvs[k] = bk;
+        }
+        if (lane < k) t = fmaf(-lts[tri(k) + lane], bk, t);
+      }
+      __syncwarp();
+
+      // ---- 5. refinement: res_r = c_r - sum_c C[r][c] b_c (Dot2 over the double-float entries)
+      float sh = 0.0f, sl = 0.0f;
+#pragma unroll 4
+      for (int c = 0; c < M; c++) {
+        float eh = 0.0f, el = 0.0f;
+        if (c == lane) {
+          eh = pad ? 1.0f : Sd.h;
+          el = pad ? 0.0f : Sd.l;
+        } else if (row_lane) {
+          const int a = c < lane ? tl + c : tri(c) + lane;
+          eh = chs[a];
+          el = cls[a];
+        }
+        const float bc = bvs[c];
+        F::dot2_acc(sh, sl, eh, bc);
+        sl = fmaf(el, bc, sl);
+      }
+      t = __fadd_rn(__fsub_rn(__fsub_rn(cv.h, sh), sl), cv.l);
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float zk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
+        t = lane > k ? fmaf(-row[k], zk, t) : (lane == k ? zk : t);
+      }
+      float dmine = 0.0f, dmax = 0.0f;
+#pragma unroll 4
+      for (int k = M - 1; k >= 0; k--) {
+        const float dk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
+        dmax = fmaxf(dmax, fabsf(dk));
+        if (lane == k) dmine = dk;
+        if (lane < k) t = fmaf(-lts[tri(k) + lane], dk, t);
+      }
+
+      // ---- 6. F, error estimate, log F, likelihood terms
+      const F::df bc = warp_sum_df(prod_df(bmine, dmine, cv.h, cv.l));
+      const F::df Fd = F::sub(Sd, bc);
+      const float q = dmax / fmaxf(bmax, 1e-30f);
+      const bool bad = !ok || !(Fd.h > nngp_bfr::kMinFRel * Sd.h) || !(q * q * Sd.h <= nngp_bfr::kTolF * Fd.h);
+      if (bad && lane == 0) nngp_flag_for_fp64(job, i);
+      const F::df lf = bad ? F::df{0.0f, 0.0f} : F::log(Fd);
+      if constexpr (MODE == 0) {
+        if (!bad) {
+          if (!pad) d.B[off + lane] = (double)bmine + (double)dmine;
+          if (lane == 0) d.F[i] = F::to_double(Fd);
+        }
+        if (lane == 0) acc0 = F::add(acc0, lf);
+      } else {
+        // r_v = V_iv - sum_k B_k V_nb(k)v, four columns per round of gathers
+        const float2 *Vf = d.Vf;
+#pragma unroll 1
+        for (int v0 = 0; v0 < nv; v0 += 4) {
+          float2 qv[4], vi[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const bool col = v0 + j < nv;
+            qv[j] = (!pad && col) ? Vf[(size_t)nbk * nv + v0 + j] : make_float2(0.0f, 0.0f);
+            vi[j] = col ? Vf[(size_t)i * nv + v0 + j] : make_float2(0.0f, 0.0f);
+          }
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            if (v0 + j < nv) {
+              const F::df s = warp_sum_df(prod_df(bmine, dmine, qv[j].x, qv[j].y));
+              const F::df rv = F::sub(F::df{vi[j].x, vi[j].y}, s);
+              if (lane == 0) {
+                rvs[2 * (v0 + j)] = rv.h;
+                rvs[2 * (v0 + j) + 1] = rv.l;
+              }
+            }
+          }
+        }
+        __syncwarp();
+        const F::df invF = bad ? F::df{0.0f, 0.0f} : F::recip(Fd);
+        // lane t: value t of the location (0: log F; then r_a r_b / F over a <= b, row-major)
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+          const int tt = lane + 32 * s;
+          if (tt < ng) {
+            F::df val = lf;
+            if (tt > 0) {
+              int rem = tt - 1, a = 0;
+              while (rem >= nv - a) {
+                rem -= nv - a;
+                a++;
+              }
+              const int c = a + rem;
+              const F::df ta = F::mul(F::df{rvs[2 * a], rvs[2 * a + 1]}, invF);
+              val = bad ? F::df{0.0f, 0.0f} : F::mul(ta, F::df{rvs[2 * c], rvs[2 * c + 1]});
+            }
+            if (s == 0) acc0 = F::add(acc0, val);
+            else acc1 = F::add(acc1, val);
+          }
+        }
+      }
+      __syncwarp();  // the warp's buffers are rewritten by the next location
+    }
+    if (lane < ng) job.partial[(size_t)tj * ng + lane] = F::to_double(acc0);
+    if (lane + 32 < ng) job.partial[(size_t)tj * ng + lane + 32] = F::to_double(acc1);
+  }
+}
+
+constexpr int kWarpsPerBlock = 4;
+
+// Launches the kernel on the plan's primary tiles [t0, t1) (tile = 32 locations of one job):
+// blocks of four warps, one tile per warp.
+template <int M, int MODE, int COV>
+int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  if (t1 <= t0) return NNGP_OK;
+  const size_t smem = sizeof(float) * WShape<M>::WARP_FLOATS * kWarpsPerBlock;
+  const int grid = (t1 - t0 + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  bfw_kernel<M, MODE, COV><<<grid, 32 * kWarpsPerBlock, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, pl->d_jobs,
+                                                                          pl->njobs, t0, t1, pl->nv);
+  NNGP_LAUNCH_CHECK(ctx);
+  return NNGP_OK;
+}
+
+}  // namespace nngp_bfw

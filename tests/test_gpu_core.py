@@ -167,14 +167,15 @@ def test_loglik_gram_matches_Q_composition(sp, orc, model, theta):
             assert abs(G[a, b] - ref) <= TOL_FP64 * max(1.0, abs(ref)) * 10
 
 
-def test_not_spd_reports_location(sp, orc):
+@pytest.mark.parametrize("m", [10, 32])
+def test_not_spd_reports_location(sp, orc, m):
     # a negative nugget larger than sigma^2 makes the first pivot negative at location 1
     rng = np.random.default_rng(3)
     c = xorder(rng.uniform(size=(200, 2)))
-    o = orc.mkNNIndxCB(cm(c), 10)
+    o = orc.mkNNIndxCB(cm(c), m)
     for prec in ("fp64", "fp32r"):
         with pytest.raises(sp.NNGPError) as e:
-            sp.updateBF(c, o[0], o[2], 10, "exponential", (1.0, -2.0, 6.0), prec)
+            sp.updateBF(c, o[0], o[2], m, "exponential", (1.0, -2.0, 6.0), prec)
         assert e.value.status == 3 and e.value.location == 1
 
 

@@ -1,6 +1,7 @@
-"""The FP32R register kernel (neighbor counts m <= 16): B, F and the fused likelihood sums
-against the FP64 form and the oracle, for every correlation model and every compiled
-neighbor bound; results independent of the launch shape the autotuner picks."""
+"""The FP32R kernels -- thread per location for m <= 16, warp per location for 16 < m <= 32:
+B, F and the fused likelihood sums against the FP64 form and the oracle, for every
+correlation model and every compiled neighbor bound; results independent of the launch shape
+the autotuner picks."""
 import numpy as np
 import pytest
 
@@ -35,7 +36,7 @@ def loglik(ld, G, beta):
 
 
 @pytest.mark.parametrize("model,theta", MODELS)
-@pytest.mark.parametrize("m", [5, 10, 12, 15, 16])
+@pytest.mark.parametrize("m", [5, 10, 12, 15, 16, 17, 20, 24, 25, 32])
 def test_fp32r_B_F_against_fp64(sp, orc, model, theta, m):
     c, X, y = dataset(3000, 10 + m)
     o = orc.mkNNIndxCB(cm(c), m)
@@ -48,7 +49,7 @@ def test_fp32r_B_F_against_fp64(sp, orc, model, theta, m):
 
 
 @pytest.mark.parametrize("model,theta", MODELS)
-@pytest.mark.parametrize("m,nv", [(10, 2), (15, 3), (16, 5)])
+@pytest.mark.parametrize("m,nv", [(10, 2), (15, 3), (16, 5), (20, 3), (32, 4), (32, 8)])
 def test_fp32r_fused_loglik_against_fp64(sp, orc, model, theta, m, nv):
     c, X, y = dataset(5000, 20 + m, nv)
     o = orc.mkNNIndxCB(cm(c), m)
@@ -131,8 +132,9 @@ def test_autotune_reports_choice(sp):
     ctx.close()
 
 
+@pytest.mark.parametrize("m", [15, 32])
 @pytest.mark.parametrize("precision", ["fp32r", "fp64"])
-def test_streamed_host_form_matches_resident_form(sp, precision):
+def test_streamed_host_form_matches_resident_form(sp, precision, m):
     """The host-pointer entry points stream their inputs in location chunks (n = 300k: 2 chunks)
     and launch the pass tile range by tile range; results are bitwise those of the
     device-pointer form, which runs the pass in one launch."""
@@ -142,7 +144,7 @@ def test_streamed_host_form_matches_resident_form(sp, precision):
 
     from spnngp_gb300._lib import _dp
 
-    n, m, nv = 300_000, 15, 3
+    n, nv = 300_000, 3
     c, X, y = dataset(n, 91, nv)
     nb = sp.mkNNIndxCB(c, m)
     nn, lu = nb["nnIndx"], nb["nnIndxLU"]
@@ -170,3 +172,34 @@ def test_streamed_host_form_matches_resident_form(sp, precision):
              prec, d_B.data_ptr(), d_F.data_ptr(), d_ld.data_ptr())
     assert np.array_equal(d_B.cpu().numpy(), B_h) and np.array_equal(d_F.cpu().numpy(), F_h)
     assert d_ld.item() == ldb_h
+
+
+@pytest.mark.parametrize("m", [20, 32])
+def test_fp32r_wide_matches_oracle_and_flags_ill_conditioned(sp, orc, m):
+    """16 < m <= 32 (the warp-per-location kernel): B, F and the fused pass against the oracle's
+    port of updateBF + Q on a well-conditioned case; and a gaussian case with a 1e-6 nugget at
+    range 0.5, whose float pivots fail or whose error estimate exceeds the bound almost
+    everywhere, against the FP64 form (F there is a 1e-6 remainder of a cancellation, so even
+    two FP64 evaluations agree only to about 1e-5: the oracle is no reference for it)."""
+    c, X, y = dataset(2500, 60 + m)
+    o = orc.mkNNIndxCB(cm(c), m)
+    V = np.column_stack([X, y])
+    beta = np.array([1.0, 0.25])
+    theta = (1.3, 0.2, 11.0)
+    Bo, Fo, ldo, st = orc.updateBF(cm(c), o[0], o[2], m, 0, *theta, 0.0)
+    assert st == 0
+    r = X @ beta - y
+    llo = -0.5 * (ldo + orc.Q(Bo, Fo, r, r, o[0], o[2]))
+    ld, G = sp.loglik_gram(c, o[0], o[2], m, V, "exponential", theta, "fp32r")
+    assert abs(loglik(ld, G, beta) - llo) <= TOL_LOGLIK * abs(llo)
+    B, F, _ = sp.updateBF(c, o[0], o[2], m, "exponential", theta, "fp32r")
+    assert np.max(np.abs(F - Fo) / Fo) <= TOL_F
+    assert np.max(np.abs(B - Bo)) <= TOL_B * max(1.0, np.max(np.abs(Bo)))
+    gau = (1.0, 1e-6, 3.462)
+    ld64, G64 = sp.loglik_gram(c, o[0], o[2], m, V, "gaussian", gau, "fp64")
+    ld32, G32 = sp.loglik_gram(c, o[0], o[2], m, V, "gaussian", gau, "fp32r")
+    assert abs(loglik(ld32, G32, beta) - loglik(ld64, G64, beta)) <= TOL_LOGLIK * abs(loglik(ld64, G64, beta))
+    B64, F64, _ = sp.updateBF(c, o[0], o[2], m, "gaussian", gau, "fp64")
+    B32, F32, _ = sp.updateBF(c, o[0], o[2], m, "gaussian", gau, "fp32r")
+    assert np.max(np.abs(F32 - F64) / F64) <= TOL_F
+    assert np.max(np.abs(B32 - B64)) <= TOL_B * max(1.0, np.max(np.abs(B64)))
