@@ -13,7 +13,10 @@ error of the FP32R form against it, the e2e throughput through the C ABI with
 host buffers (copies inside the timed region), the dominant kernel's roofline
 fraction against the measured FP32 pipe peak (and its HBM bytes against the
 measured copy bandwidth), the autotuned launch shape, and the CPU baseline (the
-oracle's C port of the reference loop, OpenMP on all host cores).
+oracle's C port of the reference loop, OpenMP on all host cores).  Sections
+(--sections): accuracy (FP32R vs FP64 at n = 1e6 for m = 15 and 32, three
+models at two ranges), mcmc (the batched multi-instance chains), conj (the
+spConjNNGP k-fold grid sweep) and serve (the request loop's p50/p99).
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
 
@@ -24,6 +27,7 @@ over all ranks divided by the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -285,6 +289,64 @@ def section_mcmc_batch(sp, ctx, dev, iters, n_inst=256, seed=77):
         "iterations_note": "the timed call includes plan building and graph capture; 5000 iterations scale "
                            "linearly from this",
     }
+
+
+# Config-1 models at effective ranges 0.05 and 0.5 (the distance where the correlation falls to
+# 0.05): exponential phi = 2.9957 / range, Matern nu = 1.5 phi = 4.7439 / range, gaussian
+# phi = 1.7308 / range with a 1e-6 nugget (the ill-conditioned case).
+ACCURACY_CASES = [("exponential", 0.05, (1.0, 0.1, 59.91)), ("exponential", 0.5, (1.0, 0.1, 5.991)),
+                  ("matern", 0.05, (1.0, 0.1, 94.88, 1.5)), ("matern", 0.5, (1.0, 0.1, 9.488, 1.5)),
+                  ("gaussian", 0.05, (1.0, 1e-6, 34.62)), ("gaussian", 0.5, (1.0, 1e-6, 3.462))]
+
+
+def section_accuracy(sp, ctx, n=N, ms=(15, 32), seed=2024):
+    """Plain method at scale, FP64 vs FP32 + refinement: n = 1e6 uniform locations, the code-book
+    neighbor search, then one updateBF and one fused log-likelihood at fixed theta for each
+    model and range; errors of the FP32R form against the FP64 form (itself pinned to the oracle
+    to 1e-10 by the tests), kernel times, and how many locations the FP32R pass re-solved in FP64."""
+    c, X, y = workload(n, seed)
+    V = np.column_stack([X, y])
+    beta = np.array([1.0, -0.5])
+    rows = []
+
+    def ll_of(ld, G):
+        return -0.5 * (ld + beta @ G[:2, :2] @ beta - 2 * beta @ G[:2, 2] + G[2, 2])
+
+    for m in ms:
+        t0 = time.perf_counter()
+        nb = sp.mkNNIndxCB(c, m, ctx=ctx)
+        knn_s = time.perf_counter() - t0
+        nn, lu = nb["nnIndx"], nb["nnIndxLU"]
+        for model, rng_eff, theta in ACCURACY_CASES:
+            res = {}
+            for prec in ("fp64", "fp32r"):
+                ctx.call("nngp_set_kernel_timing", 1)
+                ctx.call("nngp_kernel_time", None, None)
+                ld, G = sp.loglik_gram(c, nn, lu, m, V, model, theta, prec, ctx=ctx)
+                kms = C.c_double()
+                ctx.call("nngp_kernel_time", C.byref(kms), None)
+                resolved = ctx.fp32r_resolved()[0] if prec == "fp32r" else 0
+                B, F, _ = sp.updateBF(c, nn, lu, m, model, theta, prec, ctx=ctx)
+                ctx.call("nngp_set_kernel_timing", 0)
+                res[prec] = (ll_of(ld, G), B, F, kms.value, resolved)
+            ll64, B64, F64, k64, _ = res["fp64"]
+            ll32, B32, F32, k32, nres = res["fp32r"]
+            rows.append({"m": m, "model": model, "range": rng_eff, "theta": list(theta),
+                         "loglik_rel_err": abs(ll32 - ll64) / abs(ll64),
+                         "F_max_rel_err": float(np.max(np.abs(F32 - F64) / F64)),
+                         "B_max_err_rel_max_abs": float(np.max(np.abs(B32 - B64)) / max(1.0, np.max(np.abs(B64)))),
+                         "kernel_ms_fp64": k64, "kernel_ms_fp32r": k32, "fp32r_speedup": k64 / k32,
+                         "fp32r_resolved_in_fp64": nres, "knn_seconds": knn_s})
+            del B64, F64, B32, F32
+    worst = max(r["loglik_rel_err"] for r in rows)
+    return {"workload": f"n={n} uniform [0,1]^2 x-ordered, X=[1,N(0,1)], code-book neighbors, one fused "
+                        f"loglik pass and one updateBF per (m, model, range), FP32R vs FP64",
+            "cases": rows, "max_loglik_rel_err": worst,
+            "max_F_rel_err": max(r["F_max_rel_err"] for r in rows),
+            "max_B_err": max(r["B_max_err_rel_max_abs"] for r in rows),
+            "within_1e-6": bool(worst <= 1e-6 and max(r["F_max_rel_err"] for r in rows) <= 1e-6),
+            "note": "kernel_ms: the primary pass of the fused likelihood (CUDA events on the launching "
+                    "stream); the FP32R figure excludes the FP64 re-solve of the flagged locations"}
 
 
 def clustered_coords(rng, n, blobs=20, sd=0.03, uniform_frac=0.2):
@@ -627,6 +689,8 @@ def run_ours(args):
     sections = {}
     if rank == 0 and args.sections:
         clk2 = ClockSampler(dev.index).__enter__()
+        if "accuracy" in args.sections:
+            sections["accuracy"] = section_accuracy(sp, ctx)
         if "mcmc" in args.sections:
             sections["mcmc_batch"] = section_mcmc_batch(sp, ctx, dev, args.mcmc_iters)
         if "conj" in args.sections:
@@ -687,8 +751,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--sections", default="mcmc,conj,serve",
-                    help="comma-separated extra workloads reported beside the headline (mcmc, conj, serve), or ''")
+    ap.add_argument("--sections", default="accuracy,mcmc,conj,serve",
+                    help="comma-separated extra workloads reported beside the headline (accuracy, mcmc, conj, "
+                         "serve), or ''")
     ap.add_argument("--mcmc-iters", type=int, default=200)
     ap.add_argument("--launch-shape", default="",
                     help="W,G[,T]: run the FP32R register kernel with W warps per block, grid mode G and "

@@ -259,6 +259,14 @@ int nngp_measure_peak(nngp_ctx *ctx, int fp64, double *flops_per_s);
 int nngp_set_kernel_timing(nngp_ctx *ctx, int on);
 int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches);
 
+/* Precision diagnostic, no counterpart in the reference: the number of
+ * locations that the last FP32R pass of the single-dataset entry points
+ * (updateBF, loglik_gram and their _dev forms) handed to the FP64 kernel --
+ * float pivot failed, error estimate above the bound, or F below 1e-6 of
+ * sigma^2 + tau^2 -- and the number of locations that pass covered; 0 and 0
+ * after an FP64 pass.  Synchronises the context's stream. */
+int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations);
+
 /* Launch-shape autotuner of the FP32R B/F kernel for m <= 16, no counterpart
  * in the reference (it stands in for the reference's n.omp.threads tuning).
  * The first pass of a (neighbor bound, mode, correlation model, size class)

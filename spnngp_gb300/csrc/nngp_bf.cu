@@ -32,6 +32,15 @@ int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1);
 using namespace nngp_bf;
 
 namespace {
+// Number of non-zero flag bytes (grid-stride; one atomic per thread).
+__global__ void count_flags_kernel(const unsigned char *__restrict__ flags, size_t n,
+                                   unsigned long long *__restrict__ out) {
+  unsigned long long c = 0;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    c += flags[k] != 0;
+  if (c) atomicAdd(out, c);
+}
+
 // Sum over the 256 threads of a block, in a fixed tree order (every thread gets the sum).
 __device__ double block_sum256(double x, double *sbuf) {
   sbuf[threadIdx.x] = x;
@@ -506,6 +515,24 @@ int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len) {
     buf[k] = 0;
   }
   return (int)ctx->tuned.size();
+}
+int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations) {
+  if (!ctx || !resolved || !locations) return NNGP_ERR_ARG;
+  *resolved = *locations = 0;
+  const BFPlan *pl = ctx->cache_plan;
+  if (!pl || pl->precision != NNGP_FP32R || pl->flags_bytes == 0) return NNGP_OK;
+  unsigned long long *d_cnt = (unsigned long long *)nngp_malloc_async(ctx, sizeof(unsigned long long));
+  if (!d_cnt) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  unsigned long long h = 0;
+  NNGP_CUDA_TRY(ctx, cudaMemsetAsync(d_cnt, 0, sizeof h, ctx->stream));
+  count_flags_kernel<<<256, 256, 0, ctx->stream>>>(pl->d_flags, pl->flags_bytes, d_cnt);
+  NNGP_LAUNCH_CHECK(ctx);
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&h, d_cnt, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  nngp_free_async(ctx, d_cnt);
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  *resolved = (int64_t)h;
+  *locations = (int64_t)pl->flags_bytes;
+  return NNGP_OK;
 }
 int nngp_set_kernel_timing(nngp_ctx *ctx, int on) {
   ctx->timing = on != 0;

@@ -203,3 +203,20 @@ def test_fp32r_wide_matches_oracle_and_flags_ill_conditioned(sp, orc, m):
     B32, F32, _ = sp.updateBF(c, o[0], o[2], m, "gaussian", gau, "fp32r")
     assert np.max(np.abs(F32 - F64) / F64) <= TOL_F
     assert np.max(np.abs(B32 - B64)) <= TOL_B * max(1.0, np.max(np.abs(B64)))
+
+
+@pytest.mark.parametrize("m", [15, 32])
+def test_resolved_count_reports_fp64_handoffs(sp, orc, m):
+    """nngp_fp32r_resolved: a well-conditioned case re-solves (almost) nothing in FP64; the
+    gaussian with a 1e-6 nugget at range 0.5 re-solves most locations; an FP64 pass reports 0."""
+    c, X, y = dataset(4000, 80 + m)
+    o = orc.mkNNIndxCB(cm(c), m)
+    ctx = sp.default_context()
+    sp.updateBF(c, o[0], o[2], m, "exponential", (1.0, 0.1, 6.0), "fp32r")
+    r_easy, n_easy = ctx.fp32r_resolved()
+    assert n_easy == 4000 and r_easy <= 40
+    sp.updateBF(c, o[0], o[2], m, "gaussian", (1.0, 1e-6, 3.462), "fp32r")
+    r_hard, n_hard = ctx.fp32r_resolved()
+    assert n_hard == 4000 and r_hard >= 2000
+    sp.updateBF(c, o[0], o[2], m, "gaussian", (1.0, 1e-6, 3.462), "fp64")
+    assert ctx.fp32r_resolved() == (0, 0)
