@@ -299,54 +299,82 @@ ACCURACY_CASES = [("exponential", 0.05, (1.0, 0.1, 59.91)), ("exponential", 0.5,
                   ("gaussian", 0.05, (1.0, 1e-6, 34.62)), ("gaussian", 0.5, (1.0, 1e-6, 3.462))]
 
 
-def section_accuracy(sp, ctx, n=N, ms=(15, 32), seed=2024):
+def section_accuracy(sp, ctx, dev, n=N, ms=(15, 32), seed=2024, reps=3):
     """Plain method at scale, FP64 vs FP32 + refinement: n = 1e6 uniform locations, the code-book
     neighbor search, then one updateBF and one fused log-likelihood at fixed theta for each
     model and range; errors of the FP32R form against the FP64 form (itself pinned to the oracle
-    to 1e-10 by the tests), kernel times, and how many locations the FP32R pass re-solved in FP64."""
+    to 1e-10 by the tests), the time of the whole fused pass (device-resident inputs; FP32R:
+    primary kernel, FP64 re-solve of the flagged locations and the sums) after one untimed call
+    (which also tunes a new kernel class), and how many locations the FP32R pass re-solved."""
+    import torch
+
+    from spnngp_gb300._lib import _dp
+
     c, X, y = workload(n, seed)
     V = np.column_stack([X, y])
+    nv = V.shape[1]
     beta = np.array([1.0, -0.5])
     rows = []
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    d_c, d_V = t(np.ascontiguousarray(c.T).reshape(-1)), t(np.ascontiguousarray(V.T).reshape(-1))
+    d_ld = torch.zeros(1, dtype=torch.float64, device=dev)
+    d_G = torch.zeros(nv * nv, dtype=torch.float64, device=dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def ll_of(ld, G):
         return -0.5 * (ld + beta @ G[:2, :2] @ beta - 2 * beta @ G[:2, 2] + G[2, 2])
 
     for m in ms:
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         nb = sp.mkNNIndxCB(c, m, ctx=ctx)
         knn_s = time.perf_counter() - t0
         nn, lu = nb["nnIndx"], nb["nnIndxLU"]
+        d_nn, d_lu = t(nn), t(lu)
         for model, rng_eff, theta in ACCURACY_CASES:
             res = {}
-            for prec in ("fp64", "fp32r"):
+            th = np.array(list(theta) + [0.0] * (4 - len(theta)))
+            code = sp.cov_model_index(model)
+            for prec, pc in (("fp64", 0), ("fp32r", 1)):
+                def run():
+                    ctx.call("nngp_loglik_gram_dev", n, m, nv, d_c.data_ptr(), d_nn.data_ptr(), d_lu.data_ptr(),
+                             d_V.data_ptr(), code, th.ctypes.data_as(_dp), pc, d_ld.data_ptr(), d_G.data_ptr())
+                run()  # untimed: plan, tuning
+                torch.cuda.synchronize()
                 ctx.call("nngp_set_kernel_timing", 1)
                 ctx.call("nngp_kernel_time", None, None)
-                ld, G = sp.loglik_gram(c, nn, lu, m, V, model, theta, prec, ctx=ctx)
+                ev0.record()
+                for _ in range(reps):
+                    run()
+                ev1.record()
+                torch.cuda.synchronize()
                 kms = C.c_double()
                 ctx.call("nngp_kernel_time", C.byref(kms), None)
-                resolved = ctx.fp32r_resolved()[0] if prec == "fp32r" else 0
-                B, F, _ = sp.updateBF(c, nn, lu, m, model, theta, prec, ctx=ctx)
                 ctx.call("nngp_set_kernel_timing", 0)
-                res[prec] = (ll_of(ld, G), B, F, kms.value, resolved)
-            ll64, B64, F64, k64, _ = res["fp64"]
-            ll32, B32, F32, k32, nres = res["fp32r"]
+                resolved = ctx.fp32r_resolved()[0] if pc else 0
+                ll = ll_of(d_ld.item(), d_G.cpu().numpy().reshape(nv, nv))
+                B, F, _ = sp.updateBF(c, nn, lu, m, model, theta, prec, ctx=ctx)
+                res[prec] = (ll, B, F, ev0.elapsed_time(ev1) / reps, kms.value / reps, resolved)
+            ll64, B64, F64, p64, _, _ = res["fp64"]
+            ll32, B32, F32, p32, k32, nres = res["fp32r"]
             rows.append({"m": m, "model": model, "range": rng_eff, "theta": list(theta),
                          "loglik_rel_err": abs(ll32 - ll64) / abs(ll64),
                          "F_max_rel_err": float(np.max(np.abs(F32 - F64) / F64)),
                          "B_max_err_rel_max_abs": float(np.max(np.abs(B32 - B64)) / max(1.0, np.max(np.abs(B64)))),
-                         "kernel_ms_fp64": k64, "kernel_ms_fp32r": k32, "fp32r_speedup": k64 / k32,
-                         "fp32r_resolved_in_fp64": nres, "knn_seconds": knn_s})
+                         "pass_ms_fp64": p64, "pass_ms_fp32r": p32, "fp32r_speedup": p64 / p32,
+                         "fp32r_primary_kernel_ms": k32, "fp32r_resolved_in_fp64": nres, "knn_seconds": knn_s})
             del B64, F64, B32, F32
+        del d_nn, d_lu
     worst = max(r["loglik_rel_err"] for r in rows)
+    worst_f = max(r["F_max_rel_err"] for r in rows)
     return {"workload": f"n={n} uniform [0,1]^2 x-ordered, X=[1,N(0,1)], code-book neighbors, one fused "
                         f"loglik pass and one updateBF per (m, model, range), FP32R vs FP64",
-            "cases": rows, "max_loglik_rel_err": worst,
-            "max_F_rel_err": max(r["F_max_rel_err"] for r in rows),
+            "cases": rows, "max_loglik_rel_err": worst, "max_F_rel_err": worst_f,
             "max_B_err": max(r["B_max_err_rel_max_abs"] for r in rows),
-            "within_1e-6": bool(worst <= 1e-6 and max(r["F_max_rel_err"] for r in rows) <= 1e-6),
-            "note": "kernel_ms: the primary pass of the fused likelihood (CUDA events on the launching "
-                    "stream); the FP32R figure excludes the FP64 re-solve of the flagged locations"}
+            "within_1e-6": bool(worst <= 1e-6 and worst_f <= 1e-6),
+            "note": "pass_ms: the whole fused likelihood pass timed with CUDA events on the launching stream "
+                    f"(mean of {reps}); fp32r_primary_kernel_ms: its FP32R kernel alone; the gaussian cases "
+                    "(1e-6 nugget) are too ill-conditioned for a float factor and run almost entirely in FP64"}
 
 
 def clustered_coords(rng, n, blobs=20, sd=0.03, uniform_frac=0.2):
@@ -690,7 +718,7 @@ def run_ours(args):
     if rank == 0 and args.sections:
         clk2 = ClockSampler(dev.index).__enter__()
         if "accuracy" in args.sections:
-            sections["accuracy"] = section_accuracy(sp, ctx)
+            sections["accuracy"] = section_accuracy(sp, ctx, dev)
         if "mcmc" in args.sections:
             sections["mcmc_batch"] = section_mcmc_batch(sp, ctx, dev, args.mcmc_iters)
         if "conj" in args.sections:
