@@ -772,6 +772,53 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile_pass(args):
+    """One (m, model, precision, n) fused pass on resident inputs, --steps times after one untimed
+    call (plan, tuning): a short program for ncu captures of one B/F kernel."""
+    import torch
+
+    import spnngp_gb300 as sp
+    from spnngp_gb300._lib import Context, _dp
+
+    m_s, model, prec, n_s = args.profile_pass.split(",")
+    m, n = int(m_s), int(float(n_s))
+    theta = dict((r[0], r[2]) for r in ACCURACY_CASES if r[1] == 0.05)[model]
+    dev = torch.device("cuda", 0)
+    ctx = Context(0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    c, X, y = workload(n)
+    nb = sp.mkNNIndxCB(c, m, ctx=ctx)
+    V = np.column_stack([X, y])
+    nv = V.shape[1]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    d_c, d_V = t(np.ascontiguousarray(c.T).reshape(-1)), t(np.ascontiguousarray(V.T).reshape(-1))
+    d_nn, d_lu = t(nb["nnIndx"]), t(nb["nnIndxLU"])
+    d_ld = torch.zeros(1, dtype=torch.float64, device=dev)
+    d_G = torch.zeros(nv * nv, dtype=torch.float64, device=dev)
+    th = np.array(list(theta) + [0.0] * (4 - len(theta)))
+    from spnngp_gb300.core import precision_code
+
+    code, pc = sp.cov_model_index(model), precision_code(prec)
+
+    def run():
+        ctx.call("nngp_loglik_gram_dev", n, m, nv, d_c.data_ptr(), d_nn.data_ptr(), d_lu.data_ptr(), d_V.data_ptr(),
+                 code, th.ctypes.data_as(_dp), pc, d_ld.data_ptr(), d_G.data_ptr())
+
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_pass": args.profile_pass, "ms_per_pass": e0.elapsed_time(e1) / args.steps,
+                      "log_det": d_ld.item()}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -787,7 +834,13 @@ def main():
                     help="W,G[,T]: run the FP32R register kernel with W warps per block, grid mode G and "
                          "(T = 1) the tensor-memory layout instead of the autotuned shape (results are "
                          "identical for every shape)")
+    ap.add_argument("--profile-pass", default="",
+                    help="M,MODEL,PRECISION,N: only run the fused pass at that configuration --steps times (after "
+                         "one untimed call) and print its mean time -- the program for ncu captures of one kernel")
     args = ap.parse_args()
+    if args.profile_pass:
+        run_profile_pass(args)
+        return
     args.warmup = max(args.warmup, 3)
     args.sections = [x for x in args.sections.split(",") if x]
     if args.impl == "reference":

@@ -10,15 +10,18 @@
 //      common grid 2^e for the hi parts, so two hi parts subtract exactly; the quantised
 //      offsets go to the warp's shared memory, one float4 per neighbor;
 //   2. covariance in double-float (the arithmetic of the m <= 16 kernel, nngp_cov_df.cuh):
-//      lane k evaluates c_k; the pairs of the strict lower triangle are spread evenly over the
-//      lanes (pair e on lane e % 32) and stored, hi and lo parts, in the warp's triangle;
+//      lane k evaluates c_k; the pairs of the strict lower triangle are spread over the lanes
+//      by row pairs (rows t and M - 1 - t fill M - 1 lanes) and stored, hi and lo parts, at
+//      (r, c) and (c, r) of the warp's padded matrices, so lane r then reads row r at
+//      immediate offsets;
 //   3. right-looking Cholesky of the hi parts with lane r holding row r in registers: step k
 //      broadcasts the pivot and column k by shuffles (a broadcast through shared memory
 //      would take fewer instructions, but the compiler then schedules its loads into more
 //      than 255 live registers); L then goes to shared memory so that the back
 //      substitution can read its columns;
 //   4. forward and back substitution in float, one shuffle per step (lane k sends its
-//      component times its own 1 / L_kk);
+//      numerator times its own 1 / L_kk; L's zeroed diagonal and upper part make every step
+//      one fma on every lane, with no lane tests);
 //   5. one refinement step: lane r forms res_r = c_r - sum_c C[r][c] b_c over the
 //      double-float entries (a compensated Dot2 sum), and the correction delta is solved with
 //      the float factor; B = b + delta as an unevaluated float pair;
@@ -39,38 +42,27 @@ using nngp_bfr::CorDF;
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// Per-warp shared memory (floats): the geometry (32 float4), the hi and lo parts of C's strict
-// lower triangle and the float factor's strict lower triangle (row-major, (r, c) at
-// r (r - 1) / 2 + c), the exp table (32 hi, 32 lo), the float solution b and the fused pass's
-// residuals r_v (hi, lo).
+// Per-warp shared memory (floats): the geometry (32 float4); the hi and lo parts of C and the
+// float factor L as full 32 x 32 matrices with rows padded to 33 floats, (r, c) at 33 r + c,
+// so lane r reads row r and lane c reads column c at immediate offsets from its own base
+// without bank conflicts (bank (r + c) mod 32); the exp table (32 hi, 32 lo), the float
+// solution b and the fused pass's residuals r_v (hi, lo).  Entries outside the M x M block are
+// zero (set once per kernel), L's strict upper triangle and diagonal are stored as zero.
 template <int M>
 struct WShape {
-  static constexpr int NL = M * (M - 1) / 2;
-  static constexpr int NLP = (NL + 3) & ~3;
+  static constexpr int NL = M * (M - 1) / 2;  // strict lower triangle
+  static constexpr int LD = 33;
+  static constexpr int MAT = 32 * LD;
   static constexpr int GEO = 0;
   static constexpr int CH = GEO + 4 * 32;
-  static constexpr int CL = CH + NLP;
-  static constexpr int LT = CL + NLP;
-  static constexpr int TAB = LT + NLP;
+  static constexpr int CL = CH + MAT;
+  static constexpr int LT = CL + MAT;
+  static constexpr int TAB = LT + MAT;
   static constexpr int BV = TAB + 64;
   static constexpr int RV = BV + 32;
   static constexpr int WARP_FLOATS = (RV + 2 * NNGP_MAX_NV + 3) & ~3;
 };
 
-__device__ __forceinline__ constexpr int tri(int r) { return r * (r - 1) / 2; }
-
-// (r, c) of strict-lower-triangle entry e (e = tri(r) + c, c < r)
-__device__ __forceinline__ void pair_of(int e, int &r, int &c) {
-  r = (int)((1.0f + sqrtf((float)(8 * e + 1))) * 0.5f);
-  c = e - tri(r);
-  if (c < 0) {
-    r--;
-    c += r;
-  } else if (c >= r) {
-    c -= r;
-    r++;
-  }
-}
 
 // Sum over the warp of a double-float value (butterfly; the double-float add is commutative,
 // so every lane ends with the same sum)
@@ -106,8 +98,9 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
   float *chs = ws + S::CH, *cls = ws + S::CL, *lts = ws + S::LT, *tab = ws + S::TAB;
   float *bvs = ws + S::BV, *rvs = ws + S::RV;
   const int ng = MODE == 0 ? 1 : 1 + nv * (nv + 1) / 2;
-  const int tl = tri(lane);  // this lane's row start in the triangles
-  const bool row_lane = lane < M;
+  const int rb = S::LD * lane;  // this lane's row in the padded matrices
+  for (int k = lane; k < 3 * S::MAT; k += 32) chs[k] = 0.0f;  // CH, CL, LT are contiguous
+  __syncwarp();
 
   for (int kt = blockIdx.x * wpb + warp; kt < tile_end - tile_begin; kt += gridDim.x * wpb) {
     const int tile = tile_begin + kt;
@@ -166,15 +159,19 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
         cv = nngp_bfr::cov_df<COV>(F::sumsq(gx.h, gx.l, gy.h, gy.l), ck, tab, cpp);
       }
       __syncwarp();
-      constexpr int NIT = (S::NL + 31) / 32;
+      // the strict lower triangle by row pairs: iteration t covers rows t and M - 1 - t, whose
+      // t + (M - 1 - t) = M - 1 pairs fill lanes 0 .. M - 2 (lane c < t: (t, c); lane c >= t:
+      // (M - 1 - t, c - t)); two iterations per packed evaluation
+      constexpr int NIT = M / 2;
 #pragma unroll 1
       for (int t = 0; t < NIT; t += 2) {
-        int e[2], r[2], c[2];
+        int r[2], c[2];
         float4 gr[2], gc[2];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-          e[u] = lane + 32 * (t + u);
-          pair_of(min(e[u], S::NL - 1), r[u], c[u]);
+          const int tt = min(t + u, NIT - 1);
+          r[u] = lane < tt ? tt : M - 1 - tt;
+          c[u] = lane < tt ? lane : min(lane - tt, M - 1);
           gr[u] = geo[r[u]];
           gc[u] = geo[c[u]];
         }
@@ -200,22 +197,25 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
         }
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-          if (e[u] < S::NL) {
+          if (t + u < NIT && lane < M - 1) {
             const bool live = r[u] < mi;  // rows past m_i are the identity's
-            chs[e[u]] = live ? v[u].h : 0.0f;
-            cls[e[u]] = live ? v[u].l : 0.0f;
+            const float vh = live ? v[u].h : 0.0f, vl = live ? v[u].l : 0.0f;
+            const int a = S::LD * r[u] + c[u], at = S::LD * c[u] + r[u];
+            chs[a] = vh;
+            chs[at] = vh;
+            cls[a] = vl;
+            cls[at] = vl;
           }
         }
       }
+      chs[rb + lane] = pad ? 1.0f : Sd.h;  // the diagonal (identity past m_i)
+      cls[rb + lane] = pad ? 0.0f : Sd.l;
       __syncwarp();
 
       // ---- 3. Cholesky of the hi parts: lane r holds row r (entries c <= r are meaningful)
       float row[M];
 #pragma unroll
-      for (int c = 0; c < M; c++) {
-        if (c == lane) row[c] = pad ? 1.0f : Sd.h;
-        else row[c] = (c < lane && row_lane) ? chs[tl + c] : 0.0f;
-      }
+      for (int c = 0; c < M; c++) row[c] = chs[rb + c];
       bool ok = true;
       float ivmine = 1.0f;  // 1 / L_rr on lane r
 #pragma unroll
@@ -231,64 +231,48 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
           for (int j = k + 1; j < M; j++) row[j] = fmaf(-lk, __shfl_sync(kFull, lk, j), row[j]);
         }
       }
-      // L to shared memory for the column reads of the back substitution
+      // the strictly lower part of row r is L's; the diagonal and the upper part (scratch) are
+      // zeroed, so the substitutions below need no per-step lane tests; the row goes to shared
+      // memory for the column reads of the back substitution
 #pragma unroll
-      for (int c = 0; c < M - 1; c++)
-        if (c < lane && row_lane) lts[tl + c] = row[c];
+      for (int c = 0; c < M; c++) {
+        row[c] = c < lane ? row[c] : 0.0f;
+        lts[rb + c] = row[c];
+      }
       __syncwarp();
 
-      // ---- 4. L z = c, L' b = z (lane r holds component r; every lane keeps b)
-      // step k: lane k's component times its 1 / L_kk, broadcast
+      // ---- 4. L z = c, L' b = z: lane r holds component r.  Step k broadcasts lane k's
+      // numerator times its 1 / L_kk; lane r's numerator is final once step r - 1 is done (the
+      // later steps subtract zero from it), so the solution is numerator x 1 / L_rr at the end.
       float t = cv.h;
 #pragma unroll
-      for (int k = 0; k < M; k++) {
-        const float zk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
-        t = lane > k ? fmaf(-row[k], zk, t) : (lane == k ? zk : t);
-      }
-      float bmine = 0.0f, bmax = 0.0f;
-#pragma unroll 4
-      for (int k = M - 1; k >= 0; k--) {
-        const float bk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
-        bmax = fmaxf(bmax, fabsf(bk));
-        if (lane == k) {
-          bmine = bk;
-          bvs[k] = bk;
-        }
-        if (lane < k) t = fmaf(-lts[tri(k) + lane], bk, t);
-      }
+      for (int k = 0; k < M; k++) t = fmaf(-row[k], __shfl_sync(kFull, __fmul_rn(t, ivmine), k), t);
+      t = __fmul_rn(t, ivmine);
+#pragma unroll 8
+      for (int k = M - 1; k >= 0; k--)
+        t = fmaf(-lts[S::LD * k + lane], __shfl_sync(kFull, __fmul_rn(t, ivmine), k), t);
+      const float bmine = __fmul_rn(t, ivmine);
+      bvs[lane] = bmine;
+      const float bmax = __int_as_float((int)__reduce_max_sync(kFull, (unsigned)__float_as_int(fabsf(bmine))));
       __syncwarp();
 
       // ---- 5. refinement: res_r = c_r - sum_c C[r][c] b_c (Dot2 over the double-float entries)
       float sh = 0.0f, sl = 0.0f;
-#pragma unroll 4
+#pragma unroll 8
       for (int c = 0; c < M; c++) {
-        float eh = 0.0f, el = 0.0f;
-        if (c == lane) {
-          eh = pad ? 1.0f : Sd.h;
-          el = pad ? 0.0f : Sd.l;
-        } else if (row_lane) {
-          const int a = c < lane ? tl + c : tri(c) + lane;
-          eh = chs[a];
-          el = cls[a];
-        }
         const float bc = bvs[c];
-        F::dot2_acc(sh, sl, eh, bc);
-        sl = fmaf(el, bc, sl);
+        F::dot2_acc(sh, sl, chs[rb + c], bc);
+        sl = fmaf(cls[rb + c], bc, sl);
       }
       t = __fadd_rn(__fsub_rn(__fsub_rn(cv.h, sh), sl), cv.l);
 #pragma unroll
-      for (int k = 0; k < M; k++) {
-        const float zk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
-        t = lane > k ? fmaf(-row[k], zk, t) : (lane == k ? zk : t);
-      }
-      float dmine = 0.0f, dmax = 0.0f;
-#pragma unroll 4
-      for (int k = M - 1; k >= 0; k--) {
-        const float dk = __shfl_sync(kFull, __fmul_rn(t, ivmine), k);
-        dmax = fmaxf(dmax, fabsf(dk));
-        if (lane == k) dmine = dk;
-        if (lane < k) t = fmaf(-lts[tri(k) + lane], dk, t);
-      }
+      for (int k = 0; k < M; k++) t = fmaf(-row[k], __shfl_sync(kFull, __fmul_rn(t, ivmine), k), t);
+      t = __fmul_rn(t, ivmine);
+#pragma unroll 8
+      for (int k = M - 1; k >= 0; k--)
+        t = fmaf(-lts[S::LD * k + lane], __shfl_sync(kFull, __fmul_rn(t, ivmine), k), t);
+      const float dmine = __fmul_rn(t, ivmine);
+      const float dmax = __int_as_float((int)__reduce_max_sync(kFull, (unsigned)__float_as_int(fabsf(dmine))));
 
       // ---- 6. F, error estimate, log F, likelihood terms
       const F::df bc = warp_sum_df(prod_df(bmine, dmine, cv.h, cv.l));
@@ -360,11 +344,19 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
 constexpr int kWarpsPerBlock = 4;
 
 // Launches the kernel on the plan's primary tiles [t0, t1) (tile = 32 locations of one job):
-// blocks of four warps, one tile per warp.
+// blocks of four warps (54.5 KB of shared memory at M = 32, four blocks per SM), one tile per
+// warp.
 template <int M, int MODE, int COV>
 int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
-  if (t1 <= t0) return NNGP_OK;
   const size_t smem = sizeof(float) * WShape<M>::WARP_FLOATS * kWarpsPerBlock;
+  static bool configured[64] = {};  // the attribute is per device
+  const int dev = ctx->device & 63;
+  if (!configured[dev]) {
+    NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(bfw_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem));
+    configured[dev] = true;
+  }
+  if (t1 <= t0) return NNGP_OK;
   const int grid = (t1 - t0 + kWarpsPerBlock - 1) / kWarpsPerBlock;
   bfw_kernel<M, MODE, COV><<<grid, 32 * kWarpsPerBlock, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, pl->d_jobs,
                                                                           pl->njobs, t0, t1, pl->nv);
