@@ -59,10 +59,11 @@ struct Shape {
   static constexpr int LLO = NC + M;          // lo parts of the strict lower triangle (!TM)
   static constexpr int GEO = NC + M + (TM ? 0 : NL);
   static constexpr int LANE = nngp_bfr_lane_floats(M, TM);
-  static constexpr int TAB = 64;              // per-warp exp table (32 hi, 32 lo)
+  static constexpr int TAB = kTabFloats;      // per-warp table (exp, Matern polynomial)
   static constexpr size_t WARP_BYTES = nngp_bfr_warp_bytes(M, TM);
   static constexpr int MAX_WPB = nngp_bfr_max_wpb(M, TM);
   static_assert(GEO + 4 * M <= LANE, "layout exceeds the lane's share");
+  static_assert(WARP_BYTES == sizeof(float) * (32 * (size_t)LANE + TAB), "warp size disagrees with the layout");
 };
 
 // Tensor-memory access (tcgen05): one 32-bit value per lane and column.  A warp reaches the
@@ -148,12 +149,7 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
     }
     const CorDF ck = cor_prepare<COV>(cpp);
     const F::df Sd{cpp->dfDiag[0], cpp->dfDiag[1]};  // the diagonal sigma^2 + tau^2
-    {  // the warp's exp table: sigma^2 2^(j/32)
-      const float2 t2 = F::kExp2Tab[lane];
-      const F::df e = F::mul(ck.S2, F::df{t2.x, t2.y});
-      tab[lane] = e.h;
-      tab[32 + lane] = e.l;
-    }
+    fill_tab<COV>(tab, ck, cpp, lane);  // the warp's exp table and Matern coefficients
     __syncwarp();
 
     // ---- 1. geometry: offsets from the location as double-float pairs whose hi parts lie on a

@@ -45,8 +45,8 @@ constexpr unsigned kFull = 0xffffffffu;
 // Per-warp shared memory (floats): the geometry (32 float4); the hi and lo parts of C and the
 // float factor L as full 32 x 32 matrices with rows padded to 33 floats, (r, c) at 33 r + c,
 // so lane r reads row r and lane c reads column c at immediate offsets from its own base
-// without bank conflicts (bank (r + c) mod 32); the exp table (32 hi, 32 lo), the float
-// solution b and the fused pass's residuals r_v (hi, lo).  Entries outside the M x M block are
+// without bank conflicts (bank (r + c) mod 32); the exp and Matern table (nngp_cov_df.cuh), the
+// float solution b and the fused pass's residuals r_v (hi, lo).  Entries outside the M x M block are
 // zero (set once per kernel), L's strict upper triangle and diagonal are stored as zero.
 template <int M>
 struct WShape {
@@ -58,7 +58,7 @@ struct WShape {
   static constexpr int CL = CH + MAT;
   static constexpr int LT = CL + MAT;
   static constexpr int TAB = LT + MAT;
-  static constexpr int BV = TAB + 64;
+  static constexpr int BV = TAB + nngp_bfr::kTabFloats;
   static constexpr int RV = BV + 32;
   static constexpr int WARP_FLOATS = (RV + 2 * NNGP_MAX_NV + 3) & ~3;
 };
@@ -104,27 +104,26 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
 
   for (int kt = blockIdx.x * wpb + warp; kt < tile_end - tile_begin; kt += gridDim.x * wpb) {
     const int tile = tile_begin + kt;
-    const BFJob job = jobs[nngp_bfr::find_job(jobs, njobs, tile)];
-    const BFData d = datas[job.data];
-    const CovParams *cpp = thetas + job.theta;
-    const int tj = tile - job.tile0;
+    // the job's and dataset's fields are read where they are used (pointers rather than copies
+    // keep the location loop's live registers down)
+    const BFJob *jp = jobs + nngp_bfr::find_job(jobs, njobs, tile);
+    const BFData *dp = datas + jp->data;
+    const CovParams *cpp = thetas + jp->theta;
+    const int tj = tile - jp->tile0;
     const CorDF ck = nngp_bfr::cor_prepare<COV>(cpp);
     const F::df Sd{cpp->dfDiag[0], cpp->dfDiag[1]};  // the diagonal sigma^2 + tau^2
-    {  // the warp's exp table: sigma^2 2^(j/32)
-      const float2 t2 = F::kExp2Tab[lane];
-      const F::df e = F::mul(ck.S2, F::df{t2.x, t2.y});
-      tab[lane] = e.h;
-      tab[32 + lane] = e.l;
-    }
+    nngp_bfr::fill_tab<COV>(tab, ck, cpp, lane);  // the warp's exp table and Matern coefficients
     __syncwarp();
     F::df acc0{0.0f, 0.0f}, acc1{0.0f, 0.0f};
-    const int i_end = min(d.n, (tj + 1) * 32);
-    const float4 *xyf = reinterpret_cast<const float4 *>(d.xyf);
+    const int n = dp->n;
+    const int i_end = min(n, (tj + 1) * 32);
+    const float4 *xyf = reinterpret_cast<const float4 *>(dp->xyf);
+    const int *nnLU = dp->nnLU;
 
 #pragma unroll 1
     for (int i = tj * 32; i < i_end; i++) {
-      const int off = d.nnLU[i];
-      const int mi = min(d.nnLU[d.n + i], M);
+      const int off = nnLU[i];
+      const int mi = min(nnLU[n + i], M);
       const bool pad = lane >= mi;  // identity row
 
       // ---- 1. geometry
@@ -132,7 +131,7 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
       F::df ox{0.0f, 0.0f}, oy{0.0f, 0.0f};
       int nbk = 0;
       if (!pad) {
-        nbk = d.nnIndx[off + lane];
+        nbk = dp->nnIndx[off + lane];
         const float4 q = xyf[nbk];
         ox = F::diff(q.x, q.z, pi4.x, pi4.z);
         oy = F::diff(q.y, q.w, pi4.y, pi4.w);
@@ -279,17 +278,17 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
       const F::df Fd = F::sub(Sd, bc);
       const float q = dmax / fmaxf(bmax, 1e-30f);
       const bool bad = !ok || !(Fd.h > nngp_bfr::kMinFRel * Sd.h) || !(q * q * Sd.h <= nngp_bfr::kTolF * Fd.h);
-      if (bad && lane == 0) nngp_flag_for_fp64(job, i);
+      if (bad && lane == 0) nngp_flag_for_fp64(*jp, i);
       const F::df lf = bad ? F::df{0.0f, 0.0f} : F::log(Fd);
       if constexpr (MODE == 0) {
         if (!bad) {
-          if (!pad) d.B[off + lane] = (double)bmine + (double)dmine;
-          if (lane == 0) d.F[i] = F::to_double(Fd);
+          if (!pad) dp->B[off + lane] = (double)bmine + (double)dmine;
+          if (lane == 0) dp->F[i] = F::to_double(Fd);
         }
         if (lane == 0) acc0 = F::add(acc0, lf);
       } else {
         // r_v = V_iv - sum_k B_k V_nb(k)v, four columns per round of gathers
-        const float2 *Vf = d.Vf;
+        const float2 *Vf = dp->Vf;
 #pragma unroll 1
         for (int v0 = 0; v0 < nv; v0 += 4) {
           float2 qv[4], vi[4];
@@ -336,8 +335,9 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
       }
       __syncwarp();  // the warp's buffers are rewritten by the next location
     }
-    if (lane < ng) job.partial[(size_t)tj * ng + lane] = F::to_double(acc0);
-    if (lane + 32 < ng) job.partial[(size_t)tj * ng + lane + 32] = F::to_double(acc1);
+    double *partial = jp->partial + (size_t)tj * ng;
+    if (lane < ng) partial[lane] = F::to_double(acc0);
+    if (lane + 32 < ng) partial[lane + 32] = F::to_double(acc1);
   }
 }
 

@@ -21,10 +21,17 @@ struct CorDF {
   nngp_df::df K;   // exp argument scale in units of ln2/32: -phi 32/ln2 (times d), gaussian -phi^2 32/ln2 (times d^2)
   nngp_df::df P;   // phi
   nngp_df::df S2;  // sigma^2
-  float pfh[9], pfl[9];  // matern nu = k + 1/2: polynomial coefficients
   int halfk;
   int model;
 };
+
+// The warp's table (floats, in shared memory): sigma^2 2^(j/32) for j < 32 (hi at j, lo at
+// 32 + j), then the Matern nu = k + 1/2 polynomial coefficients (hi at 64 + j, lo at 80 + j,
+// j <= 8).  Shared rather than in registers: the coefficients would hold 18 registers for the
+// whole pass (the compiler puts them on the stack instead).
+constexpr int kTabFloats = 96;
+constexpr int kTabPolyHi = 64;
+constexpr int kTabPolyLo = 80;
 
 // Reads the parameter set's prepared double-float constants (cov_prepare): no FP64 here.
 template <int COV>
@@ -35,14 +42,23 @@ __device__ __forceinline__ CorDF cor_prepare(const CovParams *cp) {
   k.K = nngp_df::df{cp->dfK[0], cp->dfK[1]};
   k.P = nngp_df::df{cp->dfPhi[0], cp->dfPhi[1]};
   k.S2 = nngp_df::df{cp->dfS2[0], cp->dfS2[1]};
-  if (COV == NNGP_COV_MAT_HALF || (COV == NNGP_COV_ANY && k.model == 2 && k.halfk >= 0)) {
-#pragma unroll
-    for (int j = 0; j < 9; j++) {
-      k.pfh[j] = cp->dfPoly[j][0];
-      k.pfl[j] = cp->dfPoly[j][1];
+  return k;
+}
+
+// Writes the warp's table (kTabFloats floats at tab) for parameter set cp; every lane of the
+// warp takes part, the caller synchronises the warp before the first read.
+template <int COV>
+__device__ __forceinline__ void fill_tab(float *tab, const CorDF &k, const CovParams *cp, int lane) {
+  const float2 t2 = nngp_df::kExp2Tab[lane];
+  const nngp_df::df e = nngp_df::mul(k.S2, nngp_df::df{t2.x, t2.y});
+  tab[lane] = e.h;
+  tab[32 + lane] = e.l;
+  if (COV == NNGP_COV_MAT_HALF || COV == NNGP_COV_ANY) {
+    if (lane < 9) {
+      tab[kTabPolyHi + lane] = cp->dfPoly[lane][0];
+      tab[kTabPolyLo + lane] = cp->dfPoly[lane][1];
     }
   }
-  return k;
 }
 
 // sigma^2 rho(d) in double-float from d^2 (double-float).  The exp-based models read
@@ -78,25 +94,33 @@ __device__ __forceinline__ nngp_df::df cov_df(nngp_df::df d2, const CorDF &k, co
   const F::df E = F::exp_u(u.h, u.l, tab);
   if (k.halfk <= 0) return E;
   const F::df x = F::mul(k.P, d);
-  F::df s{k.pfh[8], k.pfl[8]};
-#pragma unroll
-  for (int j = 7; j >= 0; j--)
-    if (j < k.halfk) s = F::add(F::mul(s, x), F::df{k.pfh[j], k.pfl[j]});
-    else if (j == k.halfk) s = F::df{k.pfh[j], k.pfl[j]};
+  F::df s{tab[kTabPolyHi + k.halfk], tab[kTabPolyLo + k.halfk]};
+  for (int j = k.halfk - 1; j >= 0; j--) s = F::add(F::mul(s, x), F::df{tab[kTabPolyHi + j], tab[kTabPolyLo + j]});
   return F::mul(E, s);
 }
 
-// Models whose correlation is one exp of a scaled distance take the packed path: two pairs per
-// instruction stream (Blackwell f32x2), same arithmetic as cov_df.
+// Models whose correlation is one exp of a scaled distance (times a polynomial for the
+// half-integer Matern) take the packed path: two pairs per instruction stream (Blackwell
+// f32x2), the same arithmetic as cov_df on each half.
 template <int COV>
-constexpr bool kPacked = COV == NNGP_COV_EXP || COV == NNGP_COV_GAU;
+constexpr bool kPacked = COV == NNGP_COV_EXP || COV == NNGP_COV_GAU || COV == NNGP_COV_MAT_HALF;
 
 template <int COV>
 __device__ __forceinline__ nngp_df2::df2 cov_df2(nngp_df2::df2 d2, const CorDF &k, const float *tab) {
   namespace G = nngp_df2;
   const G::df2 K{G::splat(k.K.h), G::splat(k.K.l)};
   if constexpr (COV == NNGP_COV_GAU) return G::exp_u(G::mul(K, d2), tab);
-  else return G::exp_u(G::mul(K, G::sqrt(d2)), tab);
+  const G::df2 d = G::sqrt(d2);
+  const G::df2 E = G::exp_u(G::mul(K, d), tab);
+  if constexpr (COV == NNGP_COV_MAT_HALF) {
+    if (k.halfk <= 0) return E;
+    const G::df2 x = G::mul(G::df2{G::splat(k.P.h), G::splat(k.P.l)}, d);
+    G::df2 s{G::splat(tab[kTabPolyHi + k.halfk]), G::splat(tab[kTabPolyLo + k.halfk])};
+    for (int j = k.halfk - 1; j >= 0; j--)
+      s = G::add(G::mul(s, x), G::df2{G::splat(tab[kTabPolyHi + j]), G::splat(tab[kTabPolyLo + j])});
+    return G::mul(E, s);
+  }
+  return E;
 }
 
 __device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) {

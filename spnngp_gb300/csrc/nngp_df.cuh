@@ -281,6 +281,15 @@ __device__ __forceinline__ void fast_two_sum(p2 a, p2 b, p2 &s, p2 &e) {
   s = add(a, b);
   e = sub(b, sub(s, a));
 }
+// (a.h + a.l) + (b.h + b.l), normalised (the scalar add, per half)
+__device__ __forceinline__ df2 add(df2 a, df2 b) {
+  p2 s, e;
+  two_sum(a.h, b.h, s, e);
+  e = add(e, add(a.l, b.l));
+  df2 r;
+  fast_two_sum(s, e, r.h, r.l);
+  return r;
+}
 // (a.h + a.l)(b.h + b.l), normalised
 __device__ __forceinline__ df2 mul(df2 a, df2 b) {
   const p2 p = mul(a.h, b.h);

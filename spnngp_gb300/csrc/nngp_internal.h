@@ -282,7 +282,8 @@ inline int nngp_reg_m(int precision, int mmax) {
 // and of the c vector, the lo parts of the c vector, the lo parts of the strict lower triangle
 // (only when they are not kept in tensor memory, tm = false), one float4 of geometry per
 // neighbor (the epilogue's staging of 2 NNGP_MAX_NV + 2 (1 + NV(NV+1)/2) floats reuses the
-// front); per warp a 64-float exp table.  Blocks hold at most 8 warps and 227 KB; with tm the
+// front); per warp a 96-float table (exp table, Matern polynomial coefficients).  Blocks hold
+// at most 8 warps and 227 KB; with tm the
 // warps per block are 4 or 8 (every lane quarter of the tensor memory in use).
 constexpr int nngp_bfr_lane_floats(int M, bool tm = false) {
   const int nl = M * (M - 1) / 2;
@@ -291,7 +292,7 @@ constexpr int nngp_bfr_lane_floats(int M, bool tm = false) {
   return ((raw > red ? raw : red) + 3) & ~3;
 }
 constexpr size_t nngp_bfr_warp_bytes(int M, bool tm = false) {
-  return sizeof(float) * (32 * (size_t)nngp_bfr_lane_floats(M, tm) + 64);
+  return sizeof(float) * (32 * (size_t)nngp_bfr_lane_floats(M, tm) + 96);
 }
 constexpr int nngp_bfr_max_wpb(int M, bool tm = false) {
   const int w = (int)((size_t)227 * 1024 / nngp_bfr_warp_bytes(M, tm));
