@@ -240,9 +240,9 @@ __global__ void __launch_bounds__(128) cb_kernel(int n, int m, const double *__r
   const double qu = __dadd_rn(qx, qy);
   int lo = s, hi = s;
   bool down = true, up = true;
-  // one step of the walk at sorted position t; returns false when the direction stops
-  auto visit = [&](int t) -> bool {
-    const float4 c = sf[t];
+  // one step of the walk at sorted position t (c = sf[t]); returns false when the direction
+  // stops
+  auto visit = [&](int t, const float4 c) -> bool {
     const float fx = __fsub_rn(c.x, me.x), fy = __fsub_rn(c.y, me.y);
     const float fu = fabsf(__fadd_rn(fx, fy));
     if (fu > thr.p1) return false;  // (u_q - u_j)^2 > 2 worst for sure
@@ -268,16 +268,30 @@ __global__ void __launch_bounds__(128) cb_kernel(int n, int m, const double *__r
     }
     return true;
   };
+  // The walk alternates one step down and one step up, as the reference's does; each
+  // step's decision needs its candidate, so the candidates of the next kWalkBatch steps in
+  // both directions are loaded together (loads past a stop are simply not used) and the
+  // steps then run in the reference's order on them.
+  constexpr int kWalkBatch = 4;
   while (down || up) {
-    if (lo == 0) down = false;
-    if (hi == n - 1) up = false;
-    if (down) {
-      lo--;
-      if (!visit(lo)) down = false;
+    float4 cd[kWalkBatch], cu[kWalkBatch];
+#pragma unroll
+    for (int k = 0; k < kWalkBatch; k++) {
+      cd[k] = down ? sf[max(lo - 1 - k, 0)] : me;
+      cu[k] = up ? sf[min(hi + 1 + k, n - 1)] : me;
     }
-    if (up) {
-      hi++;
-      if (!visit(hi)) up = false;
+#pragma unroll
+    for (int k = 0; k < kWalkBatch; k++) {
+      if (lo == 0) down = false;
+      if (hi == n - 1) up = false;
+      if (down) {
+        lo--;
+        if (!visit(lo, cd[k])) down = false;
+      }
+      if (up) {
+        hi++;
+        if (!visit(hi, cu[k])) up = false;
+      }
     }
   }
   for (int k = 0; k < cnt; k++) {
