@@ -26,7 +26,8 @@ enum ScratchSlot {
   S_COORDS = 0, S_NNINDX, S_NNLU, S_B, S_F, S_V, S_PARTIAL, S_RED, S_THETA, S_STATUS,
   S_U, S_V2, S_IDX, S_IDX2, S_SORT_TMP, S_XS, S_YS, S_OS, S_NNDIST, S_COORDS0,
   S_NNINDX0, S_OUT0, S_OUT1, S_OUT2, S_OUT3, S_OUT4, S_OUT5, S_STREAM_N, S_STREAM_U,
-  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_XYF, S_VF, S_NUM_SLOTS
+  S_X, S_Y, S_MISC, S_JOBS, S_DATAS, S_MISC2, S_MISC3, S_XYF, S_VF, S_GKEY, S_GKEY2, S_GJ, S_GJ2,
+  S_GXY, S_GSTART, S_GREDO, S_NUM_SLOTS
 };
 
 struct BFPlan;

@@ -216,9 +216,11 @@ __device__ __forceinline__ float lower_de(float fx, float fy, const FilterConsts
 __global__ void __launch_bounds__(128) cb_kernel(int n, int m, const double *__restrict__ xs,
                                                  const double *__restrict__ ys, const float4 *__restrict__ sf,
                                                  FilterConsts fc, int *__restrict__ nnIndx,
-                                                 double *__restrict__ nnDist, int *__restrict__ nnLU) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
+                                                 double *__restrict__ nnDist, int *__restrict__ nnLU,
+                                                 const int *__restrict__ slist, int nwork) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwork) return;
+  const int s = slist ? slist[w] : w;  // sorted position (all of them, or the listed ones)
   const float4 me = sf[s];
   const int q = __float_as_int(me.z);
   int off, cnt;
@@ -298,6 +300,165 @@ __global__ void __launch_bounds__(128) cb_kernel(int n, int m, const double *__r
     nnIndx[off + k] = il[k];
     nnDist[off + k] = __dsqrt_rn(__longlong_as_double(kl[k]));
   }
+}
+
+// ------------------------------------------------------------ grid-bucketed search
+// The code-book walk above visits every location of a diagonal strip of the u order (about
+// 4 n r candidates for a neighbor radius r), so the primary search is a uniform grid instead:
+// location q scans rings of cells around its own, outward, keeping the m smallest squared
+// distances of predecessors (j < q; each cell lists its locations by increasing index, so
+// the scan of a cell stops at the first j >= q), and stops once every unvisited cell is
+// farther than the current m-th distance.  Distances use the reference's FP64 expression.
+// Without ties this gives the reference's list -- the walk's stopping rule is exact, so the
+// reference keeps the m smallest keys, sorted -- and a query is handed to the walk when its
+// result could depend on the walk's order: two equal keys met, or the best key left out
+// within 1e-13 (relative) of the list's last one (the walk's FP64 stopping test could then
+// have decided differently from exact arithmetic).
+struct GridGeom {
+  double x0, y0, h, inv_h, slop;
+  int nx, ny;
+};
+constexpr int kGridCellPoints = 3;  // mean locations per cell
+constexpr int kGridBrute = 2048;    // locations q < kGridBrute scan their q predecessors directly
+
+__device__ __forceinline__ int grid_coord(double v, double v0, double inv_h, int nc) {
+  const int c = (int)floor((v - v0) * inv_h);
+  return min(max(c, 0), nc - 1);
+}
+
+__global__ void grid_key_kernel(const double *__restrict__ cm, int n, GridGeom g, int *__restrict__ key,
+                                int *__restrict__ val) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    key[i] = grid_coord(cm[n + i], g.y0, g.inv_h, g.ny) * g.nx + grid_coord(cm[i], g.x0, g.inv_h, g.nx);
+    val[i] = i;
+  }
+}
+
+// start[c] = first sorted position whose cell is >= c (c = 0 .. ncells)
+__global__ void grid_start_kernel(const int *__restrict__ key, int n, int ncells, int *__restrict__ start) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int prev = p ? key[p - 1] : -1;
+  for (int c = prev + 1; c <= key[p]; c++) start[c] = p;
+  if (p == n - 1)
+    for (int c = key[p] + 1; c <= ncells; c++) start[c] = n;
+}
+
+__global__ void grid_gather_kernel(const double *__restrict__ cm, int n, const int *__restrict__ val,
+                                   double2 *__restrict__ gxy, int *__restrict__ gj) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) {
+    const int j = val[p];
+    gxy[p] = make_double2(cm[j], cm[n + j]);
+    gj[p] = j;
+  }
+}
+
+__global__ void __launch_bounds__(128) grid_knn_kernel(int n, int m, const double *__restrict__ cm, GridGeom g,
+                                                       const int *__restrict__ start,
+                                                       const double2 *__restrict__ gxy, const int *__restrict__ gj,
+                                                       int *__restrict__ nnIndx, double *__restrict__ nnDist,
+                                                       int *__restrict__ nnLU, int *__restrict__ redo,
+                                                       int *__restrict__ redo_count) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int off, cnt;
+  nn_slot(q, m, off, cnt);
+  nnLU[q] = off;
+  nnLU[n + q] = cnt;
+  if (cnt == 0) return;
+  const double qx = cm[q], qy = cm[n + q];
+  double kd[NNGP_MAX_M_SEARCH];
+  int il[NNGP_MAX_M_SEARCH];
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  int have = 0;
+  double worst = inf;  // the list's last key once it is full
+  double next = inf;   // the smallest key left out (rejected or evicted)
+  bool tie = false;
+  auto consider = [&](int j, double xj, double yj) {
+    const double dx = __dadd_rn(qx, -xj), dy = __dadd_rn(qy, -yj);
+    const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    if (have == cnt && !(de < worst)) {
+      tie |= de == worst;
+      next = fmin(next, de);
+      return;
+    }
+    int t;
+    if (have == cnt) {
+      next = fmin(next, kd[cnt - 1]);
+      t = cnt - 1;
+    } else {
+      t = have++;
+    }
+    while (t > 0 && kd[t - 1] > de) {
+      kd[t] = kd[t - 1];
+      il[t] = il[t - 1];
+      t--;
+    }
+    tie |= t > 0 && kd[t - 1] == de;
+    kd[t] = de;
+    il[t] = j;
+    if (have == cnt) worst = kd[cnt - 1];
+  };
+  if (q < kGridBrute) {
+    for (int j = 0; j < q; j++) consider(j, cm[j], cm[n + j]);
+  } else {
+    const int cx = grid_coord(qx, g.x0, g.inv_h, g.nx), cy = grid_coord(qy, g.y0, g.inv_h, g.ny);
+    auto scan = [&](int c) {
+      const int pe = start[c + 1];
+      for (int p = start[c]; p < pe; p++) {
+        const int j = gj[p];
+        if (j >= q) break;
+        const double2 v = gxy[p];
+        consider(j, v.x, v.y);
+      }
+    };
+    for (int k = 0;; k++) {
+      // ring k: the cells at Chebyshev distance k, clipped to the grid
+      const int ylo = max(cy - k, 0), yhi = min(cy + k, g.ny - 1);
+      const int xlo = max(cx - k, 0), xhi = min(cx + k, g.nx - 1);
+      for (int yy = ylo; yy <= yhi; yy++) {
+        const int row = yy * g.nx;
+        if (yy == cy - k || yy == cy + k) {
+          for (int xx = xlo; xx <= xhi; xx++) scan(row + xx);
+        } else {
+          if (cx - k >= 0) scan(row + cx - k);
+          if (k > 0 && cx + k < g.nx) scan(row + cx + k);
+        }
+      }
+      // distance from q to the cells outside the searched box (none beyond a grid edge)
+      double lb = inf;
+      if (cx - k > 0) lb = fmin(lb, qx - (g.x0 + (cx - k) * g.h));
+      if (cx + k < g.nx - 1) lb = fmin(lb, (g.x0 + (cx + k + 1) * g.h) - qx);
+      if (cy - k > 0) lb = fmin(lb, qy - (g.y0 + (cy - k) * g.h));
+      if (cy + k < g.ny - 1) lb = fmin(lb, (g.y0 + (cy + k + 1) * g.h) - qy);
+      if (lb == inf) break;  // the box covers the grid
+      if (have == cnt) {
+        const double l = lb - g.slop;
+        if (l > 0.0 && l * l > worst * (1.0 + 1e-12)) break;
+      }
+    }
+  }
+  if (tie || (have == cnt && next <= worst * (1.0 + 1e-13))) {
+    redo[atomicAdd(redo_count, 1)] = q;
+    return;
+  }
+  for (int k = 0; k < cnt; k++) {
+    nnIndx[off + k] = il[k];
+    nnDist[off + k] = __dsqrt_rn(kd[k]);
+  }
+}
+
+// pos_of[location] = sorted position (os: sorted position -> location)
+__global__ void inverse_kernel(const int *__restrict__ os, int n, int *__restrict__ pos_of) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) pos_of[os[s]] = s;
+}
+__global__ void redo_list_kernel(const int *__restrict__ pos_of, const int *__restrict__ redo_q, int nredo,
+                                 int *__restrict__ redo_s) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < nredo) redo_s[w] = pos_of[redo_q[w]];
 }
 
 // Exhaustive ordered search, location i scans j = 0..i-1 on the Euclidean distance.
@@ -541,13 +702,94 @@ int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *
   int st = check_nn_args(ctx, n, m);
   if (st) return st;
   cudaSetDevice(ctx->device);
-  double *xs, *ys;
-  int *os;
-  float4 *sf;
-  FilterConsts fc;
-  if ((st = sorted_view(ctx, n, coords, &xs, &ys, &os, nullptr, true, &sf, fc))) return st;
-  cb_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, xs, ys, sf, fc, nnIndx, nnDist, nnIndxLU);
+  // the grid over the coordinates' extent
+  unsigned long long *ext;
+  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
+  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(coords, n, ext);
   NNGP_LAUNCH_CHECK(ctx);
+  unsigned long long hk[4];
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  auto hval = [](unsigned long long k) {
+    unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    double v;
+    memcpy(&v, &b, sizeof v);
+    return v;
+  };
+  const double mnx = hval(hk[0]), mxx = hval(hk[1]), mny = hval(hk[2]), mxy = hval(hk[3]);
+  const double W = mxx - mnx, H = mxy - mny, span = std::max(W, H);
+  int *redo_q = nullptr;
+  int nredo = n;  // every location by the walk unless the grid runs
+  if (n > kGridBrute && std::isfinite(W) && std::isfinite(H) && span > 0.0) {
+    GridGeom g;
+    const double area = std::max(W, 1e-3 * span) * std::max(H, 1e-3 * span);
+    g.h = std::sqrt(area * kGridCellPoints / n);
+    for (;;) {
+      g.nx = (int)std::min(W / g.h, 1e9) + 1;
+      g.ny = (int)std::min(H / g.h, 1e9) + 1;
+      if ((long long)g.nx * g.ny <= 4LL * n + 64) break;
+      g.h *= 1.25;
+    }
+    g.x0 = mnx;
+    g.y0 = mny;
+    g.inv_h = 1.0 / g.h;
+    const double M = std::max(std::max(std::fabs(mnx), std::fabs(mxx)), std::max(std::fabs(mny), std::fabs(mxy)));
+    g.slop = 1e-7 * g.h + 1e-13 * M;  // rounding of the cell assignment and of the box edges
+    const int ncells = g.nx * g.ny;
+    int *key, *key2, *val, *val2, *start, *gj, *cnt_d;
+    double2 *gxy;
+    NNGP_ALLOC(ctx, key, int, S_GKEY, (size_t)n);
+    NNGP_ALLOC(ctx, key2, int, S_GKEY2, (size_t)n);
+    NNGP_ALLOC(ctx, val, int, S_GJ, (size_t)n);
+    NNGP_ALLOC(ctx, val2, int, S_GJ2, (size_t)n);
+    NNGP_ALLOC(ctx, gxy, double2, S_GXY, (size_t)n);
+    NNGP_ALLOC(ctx, start, int, S_GSTART, (size_t)ncells + 1);
+    NNGP_ALLOC(ctx, redo_q, int, S_GREDO, (size_t)n + 1);
+    cnt_d = redo_q + n;
+    grid_key_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(coords, n, g, key, val);
+    NNGP_LAUNCH_CHECK(ctx);
+    int bits = 1;
+    while ((1LL << bits) < ncells) bits++;
+    size_t tmp = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp, key, key2, val, val2, n, 0, bits, ctx->stream);
+    void *dtmp;
+    NNGP_ALLOC(ctx, dtmp, unsigned char, S_SORT_TMP, tmp);
+    NNGP_CUDA_TRY(ctx, cub::DeviceRadixSort::SortPairs(dtmp, tmp, key, key2, val, val2, n, 0, bits, ctx->stream));
+    ctx->launches += 1;
+    grid_start_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(key2, n, ncells, start);
+    NNGP_LAUNCH_CHECK(ctx);
+    grid_gather_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(coords, n, val2, gxy, val);
+    NNGP_LAUNCH_CHECK(ctx);
+    NNGP_CUDA_TRY(ctx, cudaMemsetAsync(cnt_d, 0, sizeof(int), ctx->stream));
+    grid_knn_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, coords, g, start, gxy, val, nnIndx, nnDist,
+                                                               nnIndxLU, redo_q, cnt_d);
+    NNGP_LAUNCH_CHECK(ctx);
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&nredo, cnt_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  if (nredo > 0) {
+    // the code-book walk: every location (small or degenerate inputs), or the listed ones
+    double *xs, *ys;
+    int *os;
+    float4 *sf;
+    FilterConsts fc;
+    if ((st = sorted_view(ctx, n, coords, &xs, &ys, &os, nullptr, true, &sf, fc))) return st;
+    int *redo_s = nullptr;
+    if (redo_q) {
+      int *pos_of;
+      NNGP_ALLOC(ctx, pos_of, int, S_GKEY, (size_t)n);
+      NNGP_ALLOC(ctx, redo_s, int, S_GKEY2, (size_t)nredo);
+      inverse_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(os, n, pos_of);
+      NNGP_LAUNCH_CHECK(ctx);
+      redo_list_kernel<<<blocks(nredo, 256), 256, 0, ctx->stream>>>(pos_of, redo_q, nredo, redo_s);
+      NNGP_LAUNCH_CHECK(ctx);
+    }
+    cb_kernel<<<blocks(nredo, 128), 128, 0, ctx->stream>>>(n, m, xs, ys, sf, fc, nnIndx, nnDist, nnIndxLU, redo_s,
+                                                           nredo);
+    NNGP_LAUNCH_CHECK(ctx);
+  }
   NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return NNGP_OK;
 }

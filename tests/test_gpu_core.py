@@ -49,7 +49,41 @@ def test_knn_cb_random(sp, orc, n, m, seed):
     assert np.array_equal(g["nnIndxLU"], o[2])
 
 
-@pytest.mark.parametrize("k", [12, 30])
+def _knn_case(kind, n, rng):
+    if kind == "uniform":
+        return xorder(rng.uniform(size=(n, 2)))
+    if kind == "clustered":
+        centers = rng.uniform(0.1, 0.9, size=(20, 2))
+        lab = rng.integers(0, 20, size=n)
+        c = np.clip(centers[lab] + rng.normal(scale=0.03, size=(n, 2)), 0, 1)
+        c[: n // 5] = rng.uniform(size=(n // 5, 2))
+        return xorder(c)
+    if kind == "line":  # collinear, y constant
+        return xorder(np.column_stack([rng.uniform(size=n), np.full(n, 0.25)]))
+    if kind == "duplicates":  # every location three times
+        base = rng.uniform(size=(n // 3, 2))
+        return xorder(np.vstack([base, base, base]))
+    if kind == "utm":
+        return xorder(rng.uniform(size=(n, 2)) * [2.0e4, 1.5e4] + [4.2e5, 4.6e6])
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("kind,n,m", [("uniform", 60_000, 15), ("uniform", 20_000, 32), ("clustered", 30_000, 15),
+                                      ("line", 12_000, 10), ("duplicates", 9_000, 12), ("utm", 25_000, 20),
+                                      ("uniform", 2_049, 15), ("uniform", 4_000, 64)])
+def test_knn_cb_grid_matches_oracle(sp, orc, kind, n, m):
+    """Past 2048 locations the search runs on the grid (locations whose result could depend on
+    the walk's order go back to the walk): indices and distances bit-exact with the oracle's
+    port of the reference's code-book search."""
+    c = _knn_case(kind, n, np.random.default_rng(n + m))
+    g = sp.mkNNIndxCB(c, m)
+    o = orc.mkNNIndxCB(cm(c), m)
+    assert np.array_equal(g["nnIndx"], o[0])
+    assert np.array_equal(g["nnDist"], o[1])
+    assert np.array_equal(g["nnIndxLU"], o[2])
+
+
+@pytest.mark.parametrize("k", [12, 30, 70])
 def test_knn_cb_ties(sp, orc, k):
     # regular lattice in a non-x order (ties in x, in u = x + y and in distance)
     c = lattice(k)
