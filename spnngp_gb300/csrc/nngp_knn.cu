@@ -450,6 +450,68 @@ __global__ void __launch_bounds__(128) grid_knn_kernel(int n, int m, const doubl
   }
 }
 
+// Exact k nearest training locations of one prediction point on the grid, ordered by
+// (squared distance, index) like nn2_kernel: the order is total, so no case needs the walk.
+// Points outside the training extent take the nearest edge cell; the box bound stays valid.
+__global__ void __launch_bounds__(128) grid_nn2_kernel(int n0, const double *__restrict__ c0, int k, GridGeom g,
+                                                       const int *__restrict__ start,
+                                                       const double2 *__restrict__ gxy, const int *__restrict__ gj,
+                                                       int *__restrict__ outIdx, double *__restrict__ outDist) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n0) return;
+  const double qx = c0[q], qy = c0[n0 + q];
+  double dl[NNGP_MAX_M_SEARCH];
+  int il[NNGP_MAX_M_SEARCH];
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  int filled = 0;
+  const int cx = grid_coord(qx, g.x0, g.inv_h, g.nx), cy = grid_coord(qy, g.y0, g.inv_h, g.ny);
+  auto scan = [&](int c) {
+    const int pe = start[c + 1];
+    for (int p = start[c]; p < pe; p++) {
+      const int j = gj[p];
+      const double2 v = gxy[p];
+      const double dx = __dadd_rn(qx, -v.x), dy = __dadd_rn(qy, -v.y);
+      const double de = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+      if (filled == k && !(de < dl[k - 1] || (de == dl[k - 1] && j < il[k - 1]))) continue;
+      int t = filled < k ? filled++ : k - 1;
+      while (t > 0 && (dl[t - 1] > de || (dl[t - 1] == de && il[t - 1] > j))) {
+        dl[t] = dl[t - 1];
+        il[t] = il[t - 1];
+        t--;
+      }
+      dl[t] = de;
+      il[t] = j;
+    }
+  };
+  for (int r = 0;; r++) {
+    const int ylo = max(cy - r, 0), yhi = min(cy + r, g.ny - 1);
+    const int xlo = max(cx - r, 0), xhi = min(cx + r, g.nx - 1);
+    for (int yy = ylo; yy <= yhi; yy++) {
+      const int row = yy * g.nx;
+      if (yy == cy - r || yy == cy + r) {
+        for (int xx = xlo; xx <= xhi; xx++) scan(row + xx);
+      } else {
+        if (cx - r >= 0) scan(row + cx - r);
+        if (r > 0 && cx + r < g.nx) scan(row + cx + r);
+      }
+    }
+    double lb = inf;
+    if (cx - r > 0) lb = fmin(lb, qx - (g.x0 + (cx - r) * g.h));
+    if (cx + r < g.nx - 1) lb = fmin(lb, (g.x0 + (cx + r + 1) * g.h) - qx);
+    if (cy - r > 0) lb = fmin(lb, qy - (g.y0 + (cy - r) * g.h));
+    if (cy + r < g.ny - 1) lb = fmin(lb, (g.y0 + (cy + r + 1) * g.h) - qy);
+    if (lb == inf) break;
+    if (filled == k) {
+      const double l = lb - g.slop;
+      if (l > 0.0 && l * l > dl[k - 1] * (1.0 + 1e-12)) break;
+    }
+  }
+  for (int t = 0; t < k; t++) {
+    outIdx[(size_t)t * n0 + q] = il[t];
+    if (outDist) outDist[(size_t)t * n0 + q] = __dsqrt_rn(dl[t]);
+  }
+}
+
 // pos_of[location] = sorted position (os: sorted position -> location)
 __global__ void inverse_kernel(const int *__restrict__ os, int n, int *__restrict__ pos_of) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -685,6 +747,75 @@ int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **
   return NNGP_OK;
 }
 
+// Extent of column-major device coordinates (min x, max x, min y, max y); synchronises.
+int coord_extent(nngp_ctx *ctx, int n, const double *d_cm, double e[4]) {
+  unsigned long long *ext;
+  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
+  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(d_cm, n, ext);
+  NNGP_LAUNCH_CHECK(ctx);
+  unsigned long long hk[4];
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int t = 0; t < 4; t++) {
+    unsigned long long b = (hk[t] >> 63) ? (hk[t] & 0x7FFFFFFFFFFFFFFFull) : ~hk[t];
+    memcpy(&e[t], &b, sizeof(double));
+  }
+  return NNGP_OK;
+}
+
+// Builds the search grid over n locations (column-major device coordinates): cells of about
+// kGridCellPoints locations, each listing its locations by increasing index (start: cell
+// offsets, gxy / gj: coordinates and indices in cell order).  usable = false when the extent
+// is degenerate or not finite (the caller runs the walk instead).
+int build_grid(nngp_ctx *ctx, int n, const double *coords, GridGeom &g, int **start, double2 **gxy, int **gj,
+               bool &usable) {
+  double e[4];
+  int st = coord_extent(ctx, n, coords, e);
+  if (st) return st;
+  const double W = e[1] - e[0], H = e[3] - e[2], span = std::max(W, H);
+  usable = std::isfinite(W) && std::isfinite(H) && span > 0.0;
+  if (!usable) return NNGP_OK;
+  const double area = std::max(W, 1e-3 * span) * std::max(H, 1e-3 * span);
+  g.h = std::sqrt(area * kGridCellPoints / n);
+  for (;;) {
+    g.nx = (int)std::min(W / g.h, 1e9) + 1;
+    g.ny = (int)std::min(H / g.h, 1e9) + 1;
+    if ((long long)g.nx * g.ny <= 4LL * n + 64) break;
+    g.h *= 1.25;
+  }
+  g.x0 = e[0];
+  g.y0 = e[2];
+  g.inv_h = 1.0 / g.h;
+  const double M = std::max(std::max(std::fabs(e[0]), std::fabs(e[1])), std::max(std::fabs(e[2]), std::fabs(e[3])));
+  g.slop = 1e-7 * g.h + 1e-13 * M;  // rounding of the cell assignment and of the box edges
+  const int ncells = g.nx * g.ny;
+  int *key, *key2, *val, *val2;
+  NNGP_ALLOC(ctx, key, int, S_GKEY, (size_t)n);
+  NNGP_ALLOC(ctx, key2, int, S_GKEY2, (size_t)n);
+  NNGP_ALLOC(ctx, val, int, S_GJ, (size_t)n);
+  NNGP_ALLOC(ctx, val2, int, S_GJ2, (size_t)n);
+  NNGP_ALLOC(ctx, *gxy, double2, S_GXY, (size_t)n);
+  NNGP_ALLOC(ctx, *start, int, S_GSTART, (size_t)ncells + 1);
+  grid_key_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(coords, n, g, key, val);
+  NNGP_LAUNCH_CHECK(ctx);
+  int bits = 1;
+  while ((1LL << bits) < ncells) bits++;
+  size_t tmp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp, key, key2, val, val2, n, 0, bits, ctx->stream);
+  void *dtmp;
+  NNGP_ALLOC(ctx, dtmp, unsigned char, S_SORT_TMP, tmp);
+  NNGP_CUDA_TRY(ctx, cub::DeviceRadixSort::SortPairs(dtmp, tmp, key, key2, val, val2, n, 0, bits, ctx->stream));
+  ctx->launches += 1;
+  grid_start_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(key2, n, ncells, *start);
+  NNGP_LAUNCH_CHECK(ctx);
+  grid_gather_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(coords, n, val2, *gxy, val);
+  NNGP_LAUNCH_CHECK(ctx);
+  *gj = val;
+  return NNGP_OK;
+}
+
 int check_nn_args(nngp_ctx *ctx, int n, int m) {
   if (!ctx) return NNGP_ERR_ARG;
   if (n < 1 || m < 1 || m > NNGP_MAX_M_SEARCH)
@@ -702,72 +833,24 @@ int nngp_mkNNIndxCB_dev(nngp_ctx *ctx, int n, int m, const double *coords, int *
   int st = check_nn_args(ctx, n, m);
   if (st) return st;
   cudaSetDevice(ctx->device);
-  // the grid over the coordinates' extent
-  unsigned long long *ext;
-  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
-  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
-  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(coords, n, ext);
-  NNGP_LAUNCH_CHECK(ctx);
-  unsigned long long hk[4];
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  auto hval = [](unsigned long long k) {
-    unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
-    double v;
-    memcpy(&v, &b, sizeof v);
-    return v;
-  };
-  const double mnx = hval(hk[0]), mxx = hval(hk[1]), mny = hval(hk[2]), mxy = hval(hk[3]);
-  const double W = mxx - mnx, H = mxy - mny, span = std::max(W, H);
   int *redo_q = nullptr;
   int nredo = n;  // every location by the walk unless the grid runs
-  if (n > kGridBrute && std::isfinite(W) && std::isfinite(H) && span > 0.0) {
+  if (n > kGridBrute) {
     GridGeom g;
-    const double area = std::max(W, 1e-3 * span) * std::max(H, 1e-3 * span);
-    g.h = std::sqrt(area * kGridCellPoints / n);
-    for (;;) {
-      g.nx = (int)std::min(W / g.h, 1e9) + 1;
-      g.ny = (int)std::min(H / g.h, 1e9) + 1;
-      if ((long long)g.nx * g.ny <= 4LL * n + 64) break;
-      g.h *= 1.25;
-    }
-    g.x0 = mnx;
-    g.y0 = mny;
-    g.inv_h = 1.0 / g.h;
-    const double M = std::max(std::max(std::fabs(mnx), std::fabs(mxx)), std::max(std::fabs(mny), std::fabs(mxy)));
-    g.slop = 1e-7 * g.h + 1e-13 * M;  // rounding of the cell assignment and of the box edges
-    const int ncells = g.nx * g.ny;
-    int *key, *key2, *val, *val2, *start, *gj, *cnt_d;
+    int *start, *gj;
     double2 *gxy;
-    NNGP_ALLOC(ctx, key, int, S_GKEY, (size_t)n);
-    NNGP_ALLOC(ctx, key2, int, S_GKEY2, (size_t)n);
-    NNGP_ALLOC(ctx, val, int, S_GJ, (size_t)n);
-    NNGP_ALLOC(ctx, val2, int, S_GJ2, (size_t)n);
-    NNGP_ALLOC(ctx, gxy, double2, S_GXY, (size_t)n);
-    NNGP_ALLOC(ctx, start, int, S_GSTART, (size_t)ncells + 1);
-    NNGP_ALLOC(ctx, redo_q, int, S_GREDO, (size_t)n + 1);
-    cnt_d = redo_q + n;
-    grid_key_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(coords, n, g, key, val);
-    NNGP_LAUNCH_CHECK(ctx);
-    int bits = 1;
-    while ((1LL << bits) < ncells) bits++;
-    size_t tmp = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tmp, key, key2, val, val2, n, 0, bits, ctx->stream);
-    void *dtmp;
-    NNGP_ALLOC(ctx, dtmp, unsigned char, S_SORT_TMP, tmp);
-    NNGP_CUDA_TRY(ctx, cub::DeviceRadixSort::SortPairs(dtmp, tmp, key, key2, val, val2, n, 0, bits, ctx->stream));
-    ctx->launches += 1;
-    grid_start_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(key2, n, ncells, start);
-    NNGP_LAUNCH_CHECK(ctx);
-    grid_gather_kernel<<<blocks(n, 256), 256, 0, ctx->stream>>>(coords, n, val2, gxy, val);
-    NNGP_LAUNCH_CHECK(ctx);
-    NNGP_CUDA_TRY(ctx, cudaMemsetAsync(cnt_d, 0, sizeof(int), ctx->stream));
-    grid_knn_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, coords, g, start, gxy, val, nnIndx, nnDist,
-                                                               nnIndxLU, redo_q, cnt_d);
-    NNGP_LAUNCH_CHECK(ctx);
-    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&nredo, cnt_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    bool usable = false;
+    if ((st = build_grid(ctx, n, coords, g, &start, &gxy, &gj, usable))) return st;
+    if (usable) {
+      NNGP_ALLOC(ctx, redo_q, int, S_GREDO, (size_t)n + 1);
+      int *cnt_d = redo_q + n;
+      NNGP_CUDA_TRY(ctx, cudaMemsetAsync(cnt_d, 0, sizeof(int), ctx->stream));
+      grid_knn_kernel<<<blocks(n, 128), 128, 0, ctx->stream>>>(n, m, coords, g, start, gxy, gj, nnIndx, nnDist,
+                                                                 nnIndxLU, redo_q, cnt_d);
+      NNGP_LAUNCH_CHECK(ctx);
+      NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&nredo, cnt_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
   }
   if (nredo > 0) {
     // the code-book walk: every location (small or degenerate inputs), or the listed ones
@@ -848,12 +931,23 @@ int nngp_nn2_dev(nngp_ctx *ctx, int n, const double *coords, int n0, const doubl
     return nngp_fail(ctx, NNGP_ERR_ARG, "nn2 needs 1 <= k <= min(n, 64)");
   if (n0 == 0) return NNGP_OK;
   cudaSetDevice(ctx->device);
+  GridGeom g;
+  int *start, *gj;
+  double2 *gxy;
+  bool usable = false;
+  int st = build_grid(ctx, n, coords, g, &start, &gxy, &gj, usable);
+  if (st) return st;
+  if (usable) {
+    grid_nn2_kernel<<<blocks(n0, 128), 128, 0, ctx->stream>>>(n0, coords0, k, g, start, gxy, gj, nnIdx, nnDist);
+    NNGP_LAUNCH_CHECK(ctx);
+    return NNGP_OK;
+  }
+  // degenerate extent (all training locations at one point): the u-order walk
   double *xs, *ys, *us;
   int *os;
   float4 *sf;
   FilterConsts fc;
-  int st = sorted_view(ctx, n, coords, &xs, &ys, &os, &us, false, &sf, fc);
-  if (st) return st;
+  if ((st = sorted_view(ctx, n, coords, &xs, &ys, &os, &us, false, &sf, fc))) return st;
   nn2_kernel<<<blocks(n0, 128), 128, 0, ctx->stream>>>(n, xs, ys, os, us, n0, coords0, k, nnIdx, nnDist);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;

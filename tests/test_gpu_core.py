@@ -130,6 +130,28 @@ def test_nn2_exact(sp, orc, n, n0, k):
     assert np.array_equal(gd, od)
 
 
+@pytest.mark.parametrize("kind,n,n0,k", [("uniform", 40_000, 5_000, 15), ("clustered", 30_000, 4_000, 25),
+                                         ("lattice", 4_900, 3_000, 12), ("outside", 20_000, 3_000, 10)])
+def test_nn2_grid_cases(sp, orc, kind, n, n0, k):
+    """The grid search of nn2: prediction points inside and outside the training extent,
+    clustered training sets, and a lattice with exact distance ties (ordered by index)."""
+    rng = np.random.default_rng(n0 + k)
+    if kind == "lattice":
+        g = np.arange(70) / 69.0
+        c = np.array([(x, y) for x in g for y in g])
+        c0 = np.round(rng.uniform(size=(n0, 2)) * 138) / 138.0  # on the half-lattice: many ties
+    elif kind == "clustered":
+        c = _knn_case("clustered", n, rng)
+        c0 = rng.uniform(size=(n0, 2))
+    else:
+        c = rng.uniform(size=(n, 2))
+        c0 = rng.uniform(-0.5, 1.5, size=(n0, 2)) if kind == "outside" else rng.uniform(size=(n0, 2))
+    gi, gd = sp.nn2(c, c0, k)
+    oi, od = orc.nn2(c, c0, k)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gd, od)
+
+
 # ---------------------------------------------------------------- B, F and Q
 
 @pytest.mark.parametrize("k", range(5))
