@@ -13,12 +13,18 @@
 // exact Shell-sort passes are replayed on the device instead (each gap's chains
 // are independent insertion sorts, one thread per chain).
 //
+// The walk visits the whole diagonal strip |u - u_q| < sqrt(2) r of the u order
+// (about 4 n r candidates per location), so mkNNIndxCB first runs a
+// grid-bucketed search (grid_knn_kernel) that finds the same lists, and only
+// the locations whose list could depend on the walk's order (equal keys, or a
+// near-tie at the list's end) are walked.
+//
 // mkNNIndx (src/nn.cpp:63-111): exhaustive scan j = 0..i-1 per location with
 // the reference's acceptance rule on the Euclidean distance.
 //
 // nn2 (the RANN::nn2 calls of R/spConjNNGP.R:158,311, R/generics.R:642):
-// unconstrained exact kNN of prediction points against the u-sorted training
-// points with the same pruning bound, ordered by (squared distance, index).
+// unconstrained exact kNN of prediction points against the training points on
+// the same grid, ordered by (squared distance, index).
 //
 // mkUIndx (src/nn.cpp:25-56, src/util.cpp:115-185): a stable radix sort of the
 // packed neighbor entries by neighbor id gives, for each location, the
