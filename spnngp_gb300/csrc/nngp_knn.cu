@@ -178,10 +178,20 @@ __global__ void extent_kernel(const double *__restrict__ cm, int n, unsigned lon
     mny = min(mny, ky);
     mxy = max(mxy, ky);
   }
-  atomicMin(&out[0], mnx);
-  atomicMax(&out[1], mxx);
-  atomicMin(&out[2], mny);
-  atomicMax(&out[3], mxy);
+  // warp reduction first: one set of atomics per warp instead of per thread
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = min(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mxx = max(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mny = min(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxy = max(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[0], mnx);
+    atomicMax(&out[1], mxx);
+    atomicMin(&out[2], mny);
+    atomicMax(&out[3], mxy);
+  }
 }
 
 // Error bounds of the float pre-filter (unit roundoff u = 2^-24, FP64 e = 2^-53):
@@ -679,6 +689,24 @@ __global__ void reverse_segments_kernel(int n, const int *__restrict__ ulu, int 
 
 inline unsigned blocks(long cnt, int tpb) { return (unsigned)((cnt + tpb - 1) / tpb); }
 
+// Extent of column-major device coordinates (min x, max x, min y, max y); synchronises.
+int coord_extent(nngp_ctx *ctx, int n, const double *d_cm, double e[4]) {
+  unsigned long long *ext;
+  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
+  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(d_cm, n, ext);
+  NNGP_LAUNCH_CHECK(ctx);
+  unsigned long long hk[4];
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int t = 0; t < 4; t++) {
+    unsigned long long b = (hk[t] >> 63) ? (hk[t] & 0x7FFFFFFFFFFFFFFFull) : ~hk[t];
+    memcpy(&e[t], &b, sizeof(double));
+  }
+  return NNGP_OK;
+}
+
 // Sorts (u, index) and builds the sorted SoA view.  coords: device, column-major.
 int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **ys, int **os,
                 double **us, bool exact_ties, float4 **sf, FilterConsts &fc) {
@@ -720,22 +748,9 @@ int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **
     }
   }
   // extent of the coordinates for the float pre-filter's error bounds
-  unsigned long long *ext;
-  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
-  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
-  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(d_cm, n, ext);
-  NNGP_LAUNCH_CHECK(ctx);
-  unsigned long long hk[4];
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  auto hval = [](unsigned long long k) {
-    unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
-    double v;
-    memcpy(&v, &b, sizeof v);
-    return v;
-  };
-  const double mnx = hval(hk[0]), mxx = hval(hk[1]), mny = hval(hk[2]), mxy = hval(hk[3]);
+  double e[4];
+  if (int st = coord_extent(ctx, n, d_cm, e)) return st;
+  const double mnx = e[0], mxx = e[1], mny = e[2], mxy = e[3];
   const double cx = 0.5 * (mnx + mxx), cy = 0.5 * (mny + mxy);
   const double S = std::max(std::max(mxx - cx, cx - mnx), std::max(mxy - cy, cy - mny)) * (1.0 + 1e-12);
   const double M = std::max(std::max(std::fabs(mnx), std::fabs(mxx)), std::max(std::fabs(mny), std::fabs(mxy)));
@@ -750,24 +765,6 @@ int sorted_view(nngp_ctx *ctx, int n, const double *d_cm, double **xs, double **
   NNGP_LAUNCH_CHECK(ctx);
   *os = idx2;
   if (us) *us = u2;
-  return NNGP_OK;
-}
-
-// Extent of column-major device coordinates (min x, max x, min y, max y); synchronises.
-int coord_extent(nngp_ctx *ctx, int n, const double *d_cm, double e[4]) {
-  unsigned long long *ext;
-  NNGP_ALLOC(ctx, ext, unsigned long long, S_MISC3, 4);
-  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(ext, init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
-  extent_kernel<<<std::min<unsigned>(blocks(n, 256), 1024), 256, 0, ctx->stream>>>(d_cm, n, ext);
-  NNGP_LAUNCH_CHECK(ctx);
-  unsigned long long hk[4];
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(hk, ext, sizeof hk, cudaMemcpyDeviceToHost, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  for (int t = 0; t < 4; t++) {
-    unsigned long long b = (hk[t] >> 63) ? (hk[t] & 0x7FFFFFFFFFFFFFFFull) : ~hk[t];
-    memcpy(&e[t], &b, sizeof(double));
-  }
   return NNGP_OK;
 }
 
