@@ -1,4 +1,5 @@
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <type_traits>
@@ -54,30 +55,40 @@ __device__ double block_sum256(double x, double *sbuf) {
   return r;
 }
 
-// Fixed-order reduction of per-tile partials: block `job`; thread t sums tiles t, t + 256, ...
-// of each value in order, then a fixed tree over the threads.  Values are taken eight at a
-// time so each thread reads whole rows of the tile-major partial array (contiguous across the
-// warp).  With jobs_fb, the FP64 re-solve's partials of the tiles marked in fb_marks are added
-// the same way (skipped when no tile was recorded: fb_count == 0).
-__global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, const BFJob *__restrict__ jobs_fb,
-                                       const unsigned *__restrict__ fb_marks, const int *__restrict__ fb_count,
-                                       int ng, double *__restrict__ out) {
-  const BFJob job = jobs[blockIdx.x];
+// Fixed-order reduction of per-tile partials in two levels.  Level 1: block (job, b) sums
+// tiles [b C, (b + 1) C) of the job (C = kReduceChunk); thread t sums tiles t, t + 256, ... of
+// the chunk, value by value in order, then a fixed tree over the threads.  Values are taken
+// eight at a time so each thread reads whole rows of the tile-major partial array
+// (contiguous across the warp).  With jobs_fb, the FP64 re-solve's partials of the tiles marked
+// in fb_marks are summed the same way into a second slot (skipped when no tile was recorded:
+// fb_count == 0).  Level 2: the chunk sums in chunk order, the re-solve's sums added last.  A
+// job of at most C tiles gets the single-block order (x + 0.0 == x).
+constexpr int kReduceChunk = 1024;
+
+__global__ void reduce_chunks_kernel(const BFJob *__restrict__ jobs, const BFJob *__restrict__ jobs_fb,
+                                     const unsigned *__restrict__ fb_marks, const int *__restrict__ fb_count,
+                                     int ng, int nchunks, double *__restrict__ out2) {
+  const int jid = blockIdx.x / nchunks, b = blockIdx.x % nchunks;
+  const BFJob job = jobs[jid];
   __shared__ double sbuf[256];
   const bool any_fb = jobs_fb && *fb_count > 0;
+  double *o = out2 + (size_t)blockIdx.x * 2 * ng;
+  const int t0 = b * kReduceChunk;
+  const int t1 = min(job.ntiles, t0 + kReduceChunk);
   for (int v0 = 0; v0 < ng; v0 += 8) {
     double acc[8], accf[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) acc[j] = accf[j] = 0.0;
-    for (int t = threadIdx.x; t < job.ntiles; t += 256) {
+    for (int t = t0 + threadIdx.x; t < t1; t += 256) {
       const double *row = job.partial + (size_t)t * ng + v0;
 #pragma unroll
       for (int j = 0; j < 8; j++)
         if (v0 + j < ng) acc[j] += row[j];
     }
     if (any_fb) {
-      const BFJob jf = jobs_fb[blockIdx.x];
-      for (int t = threadIdx.x; t < jf.ntiles; t += 256) {
+      const BFJob jf = jobs_fb[jid];
+      const int f1 = min(jf.ntiles, t0 + kReduceChunk);
+      for (int t = t0 + threadIdx.x; t < f1; t += 256) {
         if (!fb_marks[jf.tile0 + t]) continue;
         const double *row = jf.partial + (size_t)t * ng + v0;
 #pragma unroll
@@ -87,10 +98,27 @@ __global__ void reduce_partials_kernel(const BFJob *__restrict__ jobs, const BFJ
     }
 #pragma unroll 1
     for (int j = 0; j < 8 && v0 + j < ng; j++) {
-      double s = block_sum256(acc[j], sbuf);
-      if (jobs_fb) s += block_sum256(accf[j], sbuf);
-      if (threadIdx.x == 0) out[(size_t)blockIdx.x * ng + v0 + j] = s;
+      const double s = block_sum256(acc[j], sbuf);
+      const double sf = jobs_fb ? block_sum256(accf[j], sbuf) : 0.0;
+      if (threadIdx.x == 0) {
+        o[v0 + j] = s;
+        o[ng + v0 + j] = sf;
+      }
     }
+  }
+}
+
+__global__ void reduce_final_kernel(const double *__restrict__ out2, int ng, int nchunks, bool with_fb,
+                                    double *__restrict__ out) {
+  const int jid = blockIdx.x;
+  for (int v = threadIdx.x; v < ng; v += blockDim.x) {
+    double s = 0.0, sf = 0.0;
+    for (int b = 0; b < nchunks; b++) {
+      const double *o = out2 + ((size_t)jid * nchunks + b) * 2 * ng;
+      s += o[v];
+      sf += o[ng + v];
+    }
+    out[(size_t)jid * ng + v] = with_fb ? s + sf : s;
   }
 }
 
@@ -369,6 +397,14 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
     pl->d_flags = (unsigned char *)own(fb);
     if (!pl->d_partial_fb || !pl->d_flags) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
   }
+  {
+    int most = 1;
+    for (const BFJob &j : jobs) most = std::max(most, (j.ntiles + kReduceChunk - 1) / kReduceChunk);
+    for (const BFJob &j : jobs_fb) most = std::max(most, (j.ntiles + kReduceChunk - 1) / kReduceChunk);
+    pl->red_chunks = most;
+    pl->d_partial2 = (double *)own(sizeof(double) * 2 * (size_t)pl->ng * pl->njobs * most);
+    if (!pl->d_partial2) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  }
   size_t foff = 0;
   for (size_t k = 0; k < jobs.size(); k++) {
     jobs[k].partial = pl->d_partial + reinterpret_cast<size_t>(jobs[k].partial);
@@ -451,9 +487,11 @@ int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   const bool fp32r = pl->precision == NNGP_FP32R;
   // FP32R: the FP64 re-solve of the recorded tiles, folded into the same fixed-order sums
   if (fp32r && (st = launch_pass(ctx, pl, false, true, 0, 0))) return st;
-  reduce_partials_kernel<<<pl->njobs, 256, 0, ctx->stream>>>(
+  reduce_chunks_kernel<<<pl->njobs * pl->red_chunks, 256, 0, ctx->stream>>>(
       pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr, fp32r ? pl->d_fb_words + 1 : nullptr,
-      fp32r ? (const int *)pl->d_fb_words : nullptr, pl->ng, d_out);
+      fp32r ? (const int *)pl->d_fb_words : nullptr, pl->ng, pl->red_chunks, pl->d_partial2);
+  NNGP_LAUNCH_CHECK(ctx);
+  reduce_final_kernel<<<pl->njobs, 64, 0, ctx->stream>>>(pl->d_partial2, pl->ng, pl->red_chunks, fp32r, d_out);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }

@@ -222,6 +222,10 @@ struct BFPlan {
   // FP32R: [count | marks (tiles_fb)] words and the list of FP64 tiles to re-solve
   unsigned *d_fb_words = nullptr;
   int *d_fb_list = nullptr;
+  // fixed-order reduction: the tiles of a job are summed in chunks of 1024 tiles (one block
+  // each; red_chunks is the most any job has), then the chunk sums in order
+  int red_chunks = 0;
+  double *d_partial2 = nullptr;
   unsigned long long *d_status = nullptr;
   std::vector<void *> owned;
 };
