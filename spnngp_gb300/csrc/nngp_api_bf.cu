@@ -117,9 +117,29 @@ std::vector<int> chunk_bounds(int n) {
 // as soon as its copies land (the neighbors of a location precede it in the ordering, so they
 // are in the same or an earlier chunk).  The pass is the same either way: one job over all
 // locations whose tiles are launched in pieces, so results do not depend on the chunking.
+// log det and (gram != nullptr) the nv x nv Gram from the packed sums (log F, then the upper
+// triangle a <= b row-major)
+__global__ void unpack_out_kernel(const double *__restrict__ packed, int nv, double *__restrict__ ld,
+                                  double *__restrict__ gram) {
+  const int t = threadIdx.x;
+  if (t == 0) *ld = packed[0];
+  if (!gram) return;
+  for (int k = t; k < nv * (nv + 1) / 2; k += blockDim.x) {
+    int rem = k, a = 0;
+    while (rem >= nv - a) {
+      rem -= nv - a;
+      a++;
+    }
+    const int b = a + rem;
+    gram[(size_t)b * nv + a] = packed[1 + k];
+    gram[(size_t)a * nv + b] = packed[1 + k];
+  }
+}
+
 int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_coords_cm,
                const int *d_nnIndx, const int *d_nnLU, const double *d_V_cm, const CovParams &cp,
-               int precision, double *d_B, double *d_F, double *h_out, const HostIn *hin = nullptr) {
+               int precision, double *d_B, double *d_F, double *h_out, const HostIn *hin = nullptr,
+               double *d_ld = nullptr, double *d_gram = nullptr) {
   if (precision != NNGP_FP64 && precision != NNGP_FP32R)
     return nngp_fail(ctx, NNGP_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32R)");
   double *xy, *Vrm = nullptr;
@@ -221,7 +241,13 @@ int run_single(nngp_ctx *ctx, int mode, int n, int m, int nv, const double *d_co
     if ((st = nngp_bf_primary(ctx, pl, a / tile, (b + tile - 1) / tile))) return st;
   }
   if ((st = nngp_bf_finish(ctx, pl, d_out))) return st;
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, d_out, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx->stream));
+  if (d_ld) {
+    // device outputs: unpacked on the device, no host round trip
+    unpack_out_kernel<<<1, 64, 0, ctx->stream>>>(d_out, nv, d_ld, d_gram);
+    NNGP_LAUNCH_CHECK(ctx);
+  } else {
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, d_out, sizeof(double) * ng, cudaMemcpyDeviceToHost, ctx->stream));
+  }
   return nngp_check_status(ctx, d_status, mode == 0 ? "updateBF" : "loglik_gram");
 }
 
@@ -247,12 +273,8 @@ int nngp_updateBF_dev(nngp_ctx *ctx, int n, int m, const double *coords, const i
   if (st) return st;
   cudaSetDevice(ctx->device);
   const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
-  double ld = 0.0;
-  st = run_single(ctx, 0, n, m, 0, coords, nnIndx, nnIndxLU, nullptr, cp, precision, B, F, &ld);
-  if (st) return st;
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(logDet, &ld, sizeof ld, cudaMemcpyHostToDevice, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return NNGP_OK;
+  return run_single(ctx, 0, n, m, 0, coords, nnIndx, nnIndxLU, nullptr, cp, precision, B, F, nullptr, nullptr,
+                    logDet, nullptr);
 }
 
 int nngp_loglik_gram_dev(nngp_ctx *ctx, int n, int m, int nv, const double *coords,
@@ -263,15 +285,8 @@ int nngp_loglik_gram_dev(nngp_ctx *ctx, int n, int m, int nv, const double *coor
   if (nv < 1 || nv > NNGP_MAX_NV) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= nv <= 8 required");
   cudaSetDevice(ctx->device);
   const CovParams cp = make_params(covModel, theta[0], theta[1], theta[2], covModel == 2 ? theta[3] : 0.0);
-  double packed[1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2];
-  st = run_single(ctx, 1, n, m, nv, coords, nnIndx, nnIndxLU, V, cp, precision, nullptr, nullptr, packed);
-  if (st) return st;
-  double full[NNGP_MAX_NV * NNGP_MAX_NV];
-  unpack_gram(packed + 1, nv, full);
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(logDet, packed, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(gram, full, sizeof(double) * nv * nv, cudaMemcpyHostToDevice, ctx->stream));
-  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return NNGP_OK;
+  return run_single(ctx, 1, n, m, nv, coords, nnIndx, nnIndxLU, V, cp, precision, nullptr, nullptr, nullptr,
+                    nullptr, logDet, gram);
 }
 
 int nngp_updateBF(nngp_ctx *ctx, int n, int m, const double *coords, const int *nnIndx,
