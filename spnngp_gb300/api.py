@@ -415,16 +415,16 @@ def spConjNNGP(y, X, coords, knots=None, n_neighbors=15, theta_alpha=None, sigma
         res["neighbor.info"] = {"n.neighbors": n_neighbors, "n.indx": mk_n_indx_list(nn_indx, n, n_neighbors),
                                 "nn.indx": nn_indx, "nn.indx.lu": nn_indx_lu, "ord": ord_,
                                 "nn.indx.run.time": nn_run_time}
-    # exact posterior sampling (R/spConjNNGP.R:423-436)
+    # exact posterior sampling (R/spConjNNGP.R:423-436): sigma^2 ~ IG(a, b), beta | sigma^2 ~
+    # N(bB.inv bb, sigma^2 bB.inv), tau^2 = alpha sigma^2; batched (all inverse-gamma draws,
+    # then all normals: O(n.samples p^2) work, no per-sample loop)
     if n_samples > 0:
         Lb = np.linalg.cholesky(Binv)
         bhat = Binv @ res["bb"]
-        draws = np.zeros((n_samples, p + 2))
         alpha = ta[0, 1]
-        for i in range(n_samples):
-            s2 = b / gen.gamma(a)  # rigamma(1, a, b)
-            beta = bhat + math.sqrt(s2) * (Lb @ gen.standard_normal(p))
-            draws[i] = np.concatenate([beta, [s2, alpha * s2]])
+        s2 = b / gen.gamma(a, size=n_samples)
+        beta = bhat + np.sqrt(s2)[:, None] * (gen.standard_normal((n_samples, p)) @ Lb.T)
+        draws = np.column_stack([beta, s2, alpha * s2])
         res["p.beta.theta.samples"] = draws
         if fit_rep:
             inv_o = np.argsort(ord_, kind="stable")

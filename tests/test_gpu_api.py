@@ -118,3 +118,24 @@ def test_unsupported_paths_raise():
         api.spNNGP(y, X, coords, method="latent", starting={}, tuning={}, priors={}, n_samples=1)
     with pytest.raises(ValueError):
         api.spNNGP(y, X, coords, cov_model="cubic", starting={}, tuning={}, priors={}, n_samples=1)
+
+
+def test_spConjNNGP_posterior_samples_and_replicates():
+    """Exact posterior sampling of the conjugate model at one (phi, alpha) (R/spConjNNGP.R:423-436):
+    the draws' means match the closed-form posterior means within Monte Carlo error, tau^2 is
+    alpha sigma^2, and fit.rep returns one fitted and one replicated draw per sample."""
+    from spnngp_gb300 import api
+
+    coords, X, y = data(800, 4)
+    ns = 4000
+    fit = api.spConjNNGP(y, X, coords, n_neighbors=10, theta_alpha=np.array([[6.0, 0.5]]), sigma_sq_IG=[2, 1],
+                         cov_model="exponential", n_samples=ns, fit_rep=True, seed=11)
+    d = fit["p.beta.theta.samples"]
+    p = X.shape[1]
+    assert d.shape == (ns, p + 2)
+    assert np.allclose(d[:, p + 1], 0.5 * d[:, p])
+    s2 = d[:, p]
+    assert abs(s2.mean() - fit["sigma.sq.hat"]) <= 5 * np.sqrt(fit["sigma.sq.var"] / ns)
+    sd = np.sqrt(np.diag(fit["beta.var"]))
+    assert np.all(np.abs(d[:, :p].mean(axis=0) - fit["beta.hat"]) <= 5 * sd / np.sqrt(ns))
+    assert fit["y.hat.samples"].shape == (800, ns) and fit["y.rep.samples"].shape == (800, ns)
