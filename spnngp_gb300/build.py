@@ -2,7 +2,7 @@
 
 Every translation unit is compiled in parallel, then linked into one shared
 library with the CUDA runtime linked statically.  nngp_bf_inst.cu,
-nngp_bfr_inst.cu and nngp_bfw_inst.cu are compiled once per B/F kernel variant
+nngp_bfwd_inst.cu, nngp_bfr_inst.cu and nngp_bfw_inst.cu are compiled once per B/F kernel variant
 (neighbor bound x correlation code) so the heavy kernel instantiations spread
 over all cores.  Objects go to ``_build/`` next to the
 sources; the library lands next to this file.
@@ -27,12 +27,14 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 
 
 # source -> [(object suffix, defines)]: sources compiled once per variant
-# (the shared-memory kernel of nngp_bf_inst.cu is the FP64 form; FP32R runs the register
-# kernel of nngp_bfr_inst.cu for m <= 16 and the warp-per-location kernel of nngp_bfw_inst.cu
-# for 16 < m <= 32)
+# (FP64: the shared-memory kernel of nngp_bf_inst.cu for m <= 24, the warp-per-location
+# kernel of nngp_bfwd_inst.cu for 24 < m <= 32; FP32R: the register kernel of nngp_bfr_inst.cu
+# for m <= 16, the warp-per-location kernel of nngp_bfw_inst.cu for 16 < m <= 32)
 VARIANTS = {
     "nngp_bf_inst.cu": [(f"_m{m}_c{c}", [f"-DBF_M={m}", f"-DBF_COV={c}"])
-                        for m in (16, 24, 32) for c in (0, 1, 2, 3, 4)],
+                        for m in (16, 24) for c in (0, 1, 2, 3, 4)],
+    "nngp_bfwd_inst.cu": [(f"_m{m}_c{c}", [f"-DBFWD_M={m}", f"-DBFWD_COV={c}"])
+                          for m in (32,) for c in (0, 1, 2, 3, 4)],
     "nngp_bfr_inst.cu": [(f"_m{m}_c{c}", [f"-DBFR_M={m}", f"-DBFR_COV={c}"])
                          for m in (10, 15, 16) for c in (0, 1, 2, 3, 4)],
     "nngp_bfw_inst.cu": [(f"_m{m}_c{c}", [f"-DBFW_M={m}", f"-DBFW_COV={c}"])

@@ -6,12 +6,13 @@
 #include "nngp_internal.h"
 
 // Host side of the B/F pass: plans (job tables), dispatch to the kernel
-// instantiations (nngp_bf_inst.cu: the FP64 shared-memory kernel, one object per
-// neighbor bound and correlation code; nngp_bfr_inst.cu: the register FP32R
-// kernel for m <= 16; nngp_bfw_inst.cu: the warp-per-location FP32R kernel for
+// instantiations (nngp_bf_inst.cu: the FP64 shared-memory kernel for m <= 24, one
+// object per neighbor bound and correlation code; nngp_bfwd_inst.cu: the FP64
+// warp-per-location kernel for 24 < m <= 32; nngp_bfr_inst.cu: the register FP32R kernel for
+// m <= 16; nngp_bfw_inst.cu: the warp-per-location FP32R kernel for
 // 16 < m <= 32), the autotuner of the register kernel's launch shape, and the
 // fixed-order reductions.  The kernels are documented in nngp_bf_kernel.cuh,
-// nngp_bfr_kernel.cuh and nngp_bfw_kernel.cuh.
+// nngp_bfwd_kernel.cuh, nngp_bfr_kernel.cuh and nngp_bfw_kernel.cuh.
 namespace nngp_bf {
 template <int M, int MODE, int COV>
 int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
@@ -30,6 +31,10 @@ namespace nngp_bfw {
 template <int M, int MODE, int COV>
 int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1);
 }  // namespace nngp_bfw
+namespace nngp_bfwd {
+template <int M, int MODE, int COV>
+int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
+}  // namespace nngp_bfwd
 using namespace nngp_bf;
 
 namespace {
@@ -130,8 +135,10 @@ namespace {
 template <int MODE, int COV>
 int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1) {
   if (pl->mmax <= 16) return launch_one<16, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  // 24-neighbor bound: the thread-per-location kernel still holds two blocks per SM and beats the
+  // warp form (38 against 67 ms at n = 1e6); at 32 the warp form wins (97 against 206 ms)
   if (pl->mmax <= 24) return launch_one<24, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
-  return launch_one<32, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  return nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
 }
 
 template <int MODE>

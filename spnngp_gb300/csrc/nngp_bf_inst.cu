@@ -1,5 +1,5 @@
 // Explicit instantiations of the FP64 B/F kernel launcher for one variant: neighbor bound
-// BF_M (16, 24 or 32) and correlation code BF_COV (NNGP_COV_*), both modes.  The build
+// BF_M (16 or 24) and correlation code BF_COV (NNGP_COV_*), both modes.  The build
 // compiles this file once per variant, in parallel.
 #include "nngp_bf_kernel.cuh"
 #if !defined(BF_M) || !defined(BF_COV)

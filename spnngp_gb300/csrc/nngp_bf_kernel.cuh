@@ -12,8 +12,9 @@
 // shared load per FMA.  The forward solve for c is fused into the factor loop;
 // B is the back substitution.
 //
-// This is the FP64 form (everything in double), and the FP64 re-solve of the
-// locations the FP32R kernels flag (nngp_bfr_kernel.cuh for m <= 16,
+// This is the FP64 form (everything in double) for neighbor bounds m <= 24 (the
+// 32-neighbor bound runs the warp-per-location kernel of nngp_bfwd_kernel.cuh),
+// and the FP64 re-solve of the locations the FP32R kernels flag (nngp_bfr_kernel.cuh for m <= 16,
 // nngp_bfw_kernel.cuh for 16 < m <= 32): that pass walks the list of flagged
 // tiles and solves only the flagged locations.
 //
