@@ -38,22 +38,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-__device__ __forceinline__ void record_status(unsigned long long *st, unsigned long long code,
-                                              long long loc) {
-  atomicMin(st, (code << 48) | (unsigned long long)(loc & 0xFFFFFFFFFFFFll));
-}
-
-// Finds the job owning `tile` (jobs sorted by tile0).
-__device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) {
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].tile0 <= tile) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
 template <int M>
 __host__ __device__ constexpr int tri_size() { return M * (M + 1) / 2; }
 __host__ __device__ constexpr int tri_at(int r, int c) { return r * (r + 1) / 2 + c; }
@@ -91,7 +75,7 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
   const int ntodo = tile_list ? *tile_count : tile_end - tile_begin;
   for (int kt = blockIdx.x; kt < ntodo; kt += gridDim.x) {
     const int tile = tile_list ? tile_list[kt] : tile_begin + kt;
-    const int jid = find_job(jobs, njobs, tile);
+    const int jid = nngp_find_job(jobs, njobs, tile);
     const BFJob job = jobs[jid];
     const BFData d = datas[job.data];
     const CovParams *cpp = thetas + job.theta;
@@ -202,7 +186,7 @@ __global__ void __launch_bounds__(TPB, 2) bf_kernel(const BFData *__restrict__ d
         for (int r = 0; r < k; r++) z[r] -= TRI_(k, r) * Bd[k];
       }
     }
-    if (!ok && active) record_status(status, 1, i);
+    if (!ok && active) nngp_record_status(status, 1, i);
 
     // ---- F = sigma^2 + tau^2 - B'c
     double Fi;

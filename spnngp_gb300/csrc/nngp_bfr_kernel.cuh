@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
   constexpr int kStage = 2 * NNGP_MAX_NV;  // first staging slot of the per-warp sums
 
   for (int tile = tile_begin + blockIdx.x * wpb + warp; tile < tile_end; tile += gridDim.x * wpb) {
-    const BFJob job = jobs[find_job(jobs, njobs, tile)];
+    const BFJob job = jobs[nngp_find_job(jobs, njobs, tile)];
     const BFData d = datas[job.data];
     const CovParams *cpp = thetas + job.theta;
     const int tj = tile - job.tile0;

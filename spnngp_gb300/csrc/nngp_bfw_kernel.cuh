@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
     const int tile = tile_begin + kt;
     // the job's and dataset's fields are read where they are used (pointers rather than copies
     // keep the location loop's live registers down)
-    const BFJob *jp = jobs + nngp_bfr::find_job(jobs, njobs, tile);
+    const BFJob *jp = jobs + nngp_find_job(jobs, njobs, tile);
     const BFData *dp = datas + jp->data;
     const CovParams *cpp = thetas + jp->theta;
     const int tj = tile - jp->tile0;

@@ -41,20 +41,6 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-__device__ __forceinline__ void record_status(unsigned long long *st, unsigned long long code, long long loc) {
-  atomicMin(st, (code << 48) | (unsigned long long)(loc & 0xFFFFFFFFFFFFll));
-}
-
-__device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) {
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].tile0 <= tile) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
 template <int M, int MODE, int COV>
 __global__ void __launch_bounds__(128, 3) bfwd_kernel(const BFData *__restrict__ datas,
                                                    const CovParams *__restrict__ thetas,
@@ -78,7 +64,7 @@ __global__ void __launch_bounds__(128, 3) bfwd_kernel(const BFData *__restrict__
   const int ntodo = tile_list ? *tile_count : tile_end - tile_begin;
   for (int kt = blockIdx.x * wpb + warp; kt < ntodo; kt += gridDim.x * wpb) {
     const int tile = tile_list ? tile_list[kt] : tile_begin + kt;
-    const BFJob *jp = jobs + find_job(jobs, njobs, tile);
+    const BFJob *jp = jobs + nngp_find_job(jobs, njobs, tile);
     const BFData *dp = datas + jp->data;
     const CovParams *cpp = thetas + jp->theta;
     const double sigmaSq = cpp->sigmaSq, tauSq = cpp->tauSq;
@@ -167,7 +153,7 @@ __global__ void __launch_bounds__(128, 3) bfwd_kernel(const BFData *__restrict__
 #pragma unroll 4
       for (int k = M - 1; k >= 0; k--) t = fma(-mat[kLD * k + lane], __shfl_sync(kFull, t * ivmine, k), t);
       const double bmine = t * ivmine;  // B_r on lane r (0 past m_i)
-      if (!ok && lane == 0) record_status(status, 1, i);
+      if (!ok && lane == 0) nngp_record_status(status, 1, i);
 
       // ---- F = sigma^2 - B'c + tau^2, log F, likelihood terms
       const double Fi = sigmaSq - warp_sum_d(bmine * cv) + tauSq;

@@ -1,7 +1,7 @@
 // Double-float covariance evaluation shared by the FP32R B/F kernels (nngp_bfr_kernel.cuh,
 // thread per location for m <= 16; nngp_bfw_kernel.cuh, warp per location for 16 < m <= 32):
 // the correlation functions of the reference's spCor (src/util.cpp:208-245) in float pairs on the
-// FP32 pipe, the error-control thresholds both kernels apply, and the tile -> job lookup.
+// FP32 pipe, and the error-control thresholds both kernels apply.
 #pragma once
 #include <cuda_runtime.h>
 #include "nngp_df.cuh"
@@ -121,16 +121,6 @@ __device__ __forceinline__ nngp_df2::df2 cov_df2(nngp_df2::df2 d2, const CorDF &
     return G::mul(E, s);
   }
   return E;
-}
-
-__device__ __forceinline__ int find_job(const BFJob *jobs, int njobs, int tile) {
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].tile0 <= tile) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
 }
 
 }  // namespace nngp_bfr

@@ -204,6 +204,22 @@ __device__ __forceinline__ void nngp_flag_for_fp64(const BFJob &job, int i) {
   if (atomicExch(job.fb_marks + ft, 1u) == 0u) job.fb_list[atomicAdd(job.fb_count, 1)] = ft;
 }
 
+// The job owning `tile` (jobs sorted by tile0): a binary search over the job table.
+__device__ __forceinline__ int nngp_find_job(const BFJob *jobs, int njobs, int tile) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].tile0 <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Records a failed location in the pass's status word: the smallest (code, location) wins.
+__device__ __forceinline__ void nngp_record_status(unsigned long long *st, unsigned long long code, long long loc) {
+  atomicMin(st, (code << 48) | (unsigned long long)(loc & 0xFFFFFFFFFFFFll));
+}
+
 // A prepared B/F pass over a set of (dataset, parameter set) evaluations.  The
 // job tables live on the device, so nngp_bf_run only launches kernels (it can be
 // captured into a CUDA graph).  Parameter sets are read from device memory at
