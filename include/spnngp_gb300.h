@@ -299,9 +299,13 @@ int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len);
  * m <= 32, nv <= 8; larger requests return NNGP_ERR_ARG with a message in errbuf.
  * stream is a cudaStream_t (NULL = legacy default stream); every array is a
  * device pointer except theta (host) and errbuf (host, may be NULL).  The first
- * call on a device looks up the array's address and configures the kernel, so
- * make it before any stream capture.  All calls share the array: calls whose
- * work overlaps on the GPU race and must be serialised by the caller. */
+ * call on a device looks up the array's address and configures the kernel.  No
+ * call may be made while its stream is being captured into a CUDA graph (each
+ * call copies host values and waits for its stream before returning): such a
+ * call returns NNGP_ERR_ARG.  The sums are formed in the same order as
+ * nngp_loglik_gram_dev's FP64 pass, so both give the same result.  All calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * serialised by the caller. */
 int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, const double *coords,
                              const int *nnIndx, const int *nnIndxLU, const double *V, int covModel,
                              const double *theta, double *logDet, double *gram, char *errbuf,

@@ -271,10 +271,11 @@ int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int 
   const size_t smem = sizeof(double) * ((size_t)tri_size<M>() + (size_t)2 * M) * TPB +
                       sizeof(double) * (TPB / 32) * kNGMax;
   auto kern = bf_kernel<M, MODE, TPB, COV>;
-  static bool configured = false;  // once per instantiation
-  if (!configured) {
+  static bool configured[64] = {};  // the attribute is per device
+  const int dev = ctx->device & 63;
+  if (!configured[dev]) {
     NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = true;
+    configured[dev] = true;
   }
   const int tiles = fallback_pass ? pl->tiles_fb : t1 - t0;
   const BFJob *jobs = fallback_pass ? pl->d_jobs_fb : pl->d_jobs;

@@ -17,7 +17,10 @@
 //     larger requests are rejected with NNGP_ERR_ARG and a message;
 //   - the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (and sets the kernel's shared-memory attribute);
-//     make that first call before any stream capture;
+//   - no call may be made while its stream is being captured into a CUDA graph:
+//     each call copies host stack values to the device and waits for its stream
+//     before it returns, neither of which a graph can hold; such a call returns
+//     NNGP_ERR_ARG;
 //   - all calls share the one array and it keeps the previous call's contents:
 //     the status word is reset by every call, everything else is overwritten
 //     before it is read; calls whose work overlaps on the GPU (two streams, or
@@ -39,7 +42,10 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kOffXY = 0;
 constexpr size_t kOffV = kOffXY + align256(sizeof(double) * 2 * kMaxN);
 constexpr size_t kOffPartial = kOffV + align256(sizeof(double) * (size_t)kMaxN * kMaxNV);
-constexpr size_t kOffOut = kOffPartial + align256(sizeof(double) * (size_t)kMaxTiles * kNGMax);
+// the allocating pass's two-level reduction: chunks of 1024 tiles, then the chunk sums in order
+constexpr int kMaxChunks = (kMaxTiles + 1023) / 1024;
+constexpr size_t kOffPartial2 = kOffPartial + align256(sizeof(double) * (size_t)kMaxTiles * kNGMax);
+constexpr size_t kOffOut = kOffPartial2 + align256(sizeof(double) * 2 * kNGMax * (size_t)kMaxChunks);
 constexpr size_t kOffTheta = kOffOut + align256(sizeof(double) * 2 * kNGMax);
 constexpr size_t kOffData = kOffTheta + align256(sizeof(CovParams));
 constexpr size_t kOffJob = kOffData + align256(sizeof(BFData));
@@ -67,37 +73,18 @@ __global__ void na_row_major_kernel(const double *__restrict__ cm, int n, int nv
   }
 }
 
-// Sums the per-tile partials in a fixed order and writes logDet and the full
-// nv x nv Gram into the caller's device buffers.
-__global__ void na_finish_kernel(const double *__restrict__ partial, int ntiles, int nv, double *__restrict__ logDet,
+// Writes the pass's sums (log F first, then the Gram entries a <= b, row-major) as logDet and
+// the full nv x nv Gram into the caller's device buffers.
+__global__ void na_unpack_kernel(const double *__restrict__ sums, int nv, double *__restrict__ logDet,
                                  double *__restrict__ gram) {
-  __shared__ double sbuf[256];
-  const int ng = 1 + nv * (nv + 1) / 2;
-  for (int v = 0; v < ng; v++) {
-    double s = 0.0;
-    for (int t = threadIdx.x; t < ntiles; t += 256) s += partial[(size_t)t * ng + v];
-    sbuf[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-      if (threadIdx.x < w) sbuf[threadIdx.x] += sbuf[threadIdx.x + w];
-      __syncthreads();
+  if (threadIdx.x != 0) return;
+  *logDet = sums[0];
+  int k = 1;
+  for (int a = 0; a < nv; a++)
+    for (int b = a; b < nv; b++, k++) {
+      gram[(size_t)b * nv + a] = sums[k];
+      gram[(size_t)a * nv + b] = sums[k];
     }
-    if (threadIdx.x == 0) {
-      if (v == 0) {
-        *logDet = sbuf[0];
-      } else {
-        int k = v - 1, a = 0;
-        while (k >= nv - a) {
-          k -= nv - a;
-          a++;
-        }
-        const int b = a + k;
-        gram[(size_t)b * nv + a] = sbuf[0];
-        gram[(size_t)a * nv + b] = sbuf[0];
-      }
-    }
-    __syncthreads();
-  }
 }
 
 int fail(nngp_ctx *ctx, int status, const char *msg) {
@@ -129,6 +116,14 @@ extern "C" int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, cons
   if (nv < 1 || nv > kMaxNV) return report(fail(&ctx, NNGP_ERR_ARG, "nngp_loglik_gram_noalloc: 1 <= nv <= 8 required"));
   if (covModel < 0 || covModel > 3)
     return report(fail(&ctx, NNGP_ERR_ARG, "nngp_loglik_gram_noalloc: cov.model is not correctly specified"));
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ctx.stream, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return report(fail(&ctx, NNGP_ERR_CUDA, "nngp_loglik_gram_noalloc: invalid stream"));
+  }
+  if (cap != cudaStreamCaptureStatusNone)
+    return report(fail(&ctx, NNGP_ERR_ARG,
+                       "nngp_loglik_gram_noalloc: must not be called while its stream is being captured"));
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return report(fail(&ctx, NNGP_ERR_CUDA, "nngp_loglik_gram_noalloc: no usable CUDA device"));
@@ -149,6 +144,8 @@ extern "C" int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, cons
   double *xy = (double *)(base + kOffXY);
   double *Vrm = (double *)(base + kOffV);
   double *partial = (double *)(base + kOffPartial);
+  double *partial2 = (double *)(base + kOffPartial2);
+  double *sums = (double *)(base + kOffOut);
   CovParams *d_theta = (CovParams *)(base + kOffTheta);
   BFData *d_data = (BFData *)(base + kOffData);
   BFJob *d_job = (BFJob *)(base + kOffJob);
@@ -190,6 +187,8 @@ extern "C" int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, cons
   plan.d_jobs = d_job;
   plan.d_partial = partial;
   plan.d_status = d_status;
+  plan.red_chunks = (job.ntiles + 1023) / 1024;
+  plan.d_partial2 = partial2;
 
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_theta, &cp, sizeof cp, cudaMemcpyHostToDevice, ctx.stream);
@@ -202,8 +201,9 @@ extern "C" int nngp_loglik_gram_noalloc(void *stream, int n, int m, int nv, cons
   na_row_major_kernel<<<(unsigned)(((long)n * nv + 255) / 256), 256, 0, ctx.stream>>>(V, n, nv, Vrm);
   plan.cov = nngp_plan_cov(&cp, 1);
   st = nngp_bf_launch(&ctx, &plan, false, false);
+  if (!st) st = nngp_bf_finish(&ctx, &plan, sums);  // the allocating pass's reduction, same order
   if (st) return report(st);
-  na_finish_kernel<<<1, 256, 0, ctx.stream>>>(partial, job.ntiles, nv, logDet, gram);
+  na_unpack_kernel<<<1, 32, 0, ctx.stream>>>(sums, nv, logDet, gram);
   e = cudaGetLastError();
   if (e != cudaSuccess)
     return report(fail(&ctx, NNGP_ERR_CUDA, (std::string("nngp_loglik_gram_noalloc: ") + cudaGetErrorString(e)).c_str()));

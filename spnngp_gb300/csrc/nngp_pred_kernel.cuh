@@ -258,10 +258,11 @@ int launch_pred(nngp_ctx *ctx, const PredArgs &a) {
   constexpr int GEO = R32 ? 4 : 2;
   const size_t smem = sizeof(T) * ((size_t)ptri_size<M>() + (size_t)GEO * M) * TPB;
   auto kern = pred_kernel<M, R32, KIND, TPB>;
-  static bool configured = false;
-  if (!configured) {
+  static bool configured[64] = {};  // the attribute is per device
+  const int dev = ctx->device & 63;
+  if (!configured[dev]) {
     NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = true;
+    configured[dev] = true;
   }
   const long total = (long)a.n0 * a.npar;
   if (total <= 0) return NNGP_OK;

@@ -12,7 +12,7 @@ from conftest import cm, xorder
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12  # same FP64 kernel and reduction order: agreement to rounding
+TOL = 1e-12  # same FP64 kernel and reduction order: the results agree to rounding
 
 
 def _setup(n, m, seed):
@@ -78,7 +78,9 @@ def _alloc(t, n, m, nv, model, theta):
     return out
 
 
-@pytest.mark.parametrize("n,m,model,theta", [(3000, 15, 0, (1.0, 0.1, 6.0)), (5000, 32, 2, (1.0, 0.2, 9.0, 1.5))])
+@pytest.mark.parametrize("n,m,model,theta", [(3000, 15, 0, (1.0, 0.1, 6.0)), (5000, 32, 2, (1.0, 0.2, 9.0, 1.5)),
+                                             # 1875 tiles of 32 locations: two reduction chunks of 1024 tiles
+                                             (60000, 32, 0, (1.0, 0.1, 6.0))])
 def test_noalloc_matches_allocating_pass_twice(n, m, model, theta):
     lib = _lib()
     t, nv = _setup(n, m, n + m)
@@ -99,3 +101,55 @@ def test_noalloc_rejects_oversized_requests():
     st = f(None, 70000, 15, nv, t["c"].data_ptr(), t["nn"].data_ptr(), t["lu"].data_ptr(), t["V"].data_ptr(), 0,
            th.ctypes.data_as(C.POINTER(C.c_double)), None, None, err, 256)
     assert st == 1 and b"65536" in err.value
+
+
+def test_noalloc_allocates_no_device_memory():
+    """Once warm, calls leave the device's free memory and torch's pool unchanged."""
+    import torch
+
+    lib = _lib()
+    n, m, model, theta = 20000, 15, 0, (1.0, 0.1, 6.0)
+    t, nv = _setup(n, m, 5)
+    ld = torch.zeros(1, dtype=torch.float64, device="cuda")
+    G = torch.zeros(nv * nv, dtype=torch.float64, device="cuda")
+    th = np.array(list(theta) + [0.0])
+    err = C.create_string_buffer(256)
+    f = _fn(lib)
+    args = (None, n, m, nv, t["c"].data_ptr(), t["nn"].data_ptr(), t["lu"].data_ptr(), t["V"].data_ptr(), model,
+            th.ctypes.data_as(C.POINTER(C.c_double)), ld.data_ptr(), G.data_ptr(), err, 256)
+    assert f(*args) == 0, err.value  # warm: the array's address is looked up, the kernels are loaded
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    for _ in range(3):
+        assert f(*args) == 0, err.value
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_reserved() == reserved0
+
+
+def test_noalloc_refuses_stream_capture():
+    """A call on a stream that is being captured returns NNGP_ERR_ARG and enqueues nothing."""
+    import torch
+
+    lib = _lib()
+    n, m = 3000, 15
+    t, nv = _setup(n, m, 9)
+    ld = torch.zeros(1, dtype=torch.float64, device="cuda")
+    G = torch.zeros(nv * nv, dtype=torch.float64, device="cuda")
+    th = np.array([1.0, 0.1, 6.0, 0.0])
+    err = C.create_string_buffer(256)
+    f = _fn(lib)
+    assert f(None, n, m, nv, t["c"].data_ptr(), t["nn"].data_ptr(), t["lu"].data_ptr(), t["V"].data_ptr(), 0,
+             th.ctypes.data_as(C.POINTER(C.c_double)), ld.data_ptr(), G.data_ptr(), err, 256) == 0
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+            ld.add_(0.0)
+            st = f(C.c_void_p(side.cuda_stream), n, m, nv, t["c"].data_ptr(), t["nn"].data_ptr(), t["lu"].data_ptr(),
+                   t["V"].data_ptr(), 0, th.ctypes.data_as(C.POINTER(C.c_double)), ld.data_ptr(), G.data_ptr(), err,
+                   256)
+    assert st == 1 and b"captured" in err.value
