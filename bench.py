@@ -160,13 +160,48 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, n):
+def bench_config():
+    """The workload both arms run (the same string on both lines)."""
+    return {"workload": f"n={N} uniform [0,1]^2 x-ordered (seed 2024), m={M} code-book neighbors, {COV} "
+                        f"sigma2={THETA[0]} tau2={THETA[1]} phi={THETA[2]}, X=[1,N(0,1)], one fused "
+                        f"updateBF + log-likelihood pass per step",
+            "l2": "GPU arm: flushed between timed steps (512 MB write), inputs ~100 MB; CPU arm: host memory"}
+
+
+def cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, n, keep=False):
     """One reference-path step on the host: updateBF (potrf/potri/symv per location) plus the
-    log-likelihood quadratic form Q(X beta - y), as src/rNNGP.cpp:306-317 computes them."""
-    B, F, ld, st = orc.updateBF(ccm, nn, lu, M, 0, *THETA, 0.0, threads=threads)
-    r = Xcm[:n] * 1.0 + Xcm[n:] * -0.5 - y
-    q = orc.Q(B, F, r, r, nn, lu, threads=threads)
-    return -0.5 * (ld + q)
+    log-likelihood quadratic form Q(X beta - y), as src/rNNGP.cpp:306-317 computes them.  orc is
+    the oracle port or the reference's own build (oracle.Reference); keep=True also returns B
+    and F."""
+    from oracle.oracle import Reference
+
+    if isinstance(orc, Reference):
+        B, F, ld, st = orc.updateBF(ccm, nn, lu, M, 0, np.array(THETA), threads=threads)
+        r = Xcm[:n] * 1.0 + Xcm[n:] * -0.5 - y
+        q = orc.Q(B, F, r, r, nn, lu)
+    else:
+        B, F, ld, st = orc.updateBF(ccm, nn, lu, M, 0, *THETA, 0.0, threads=threads)
+        r = Xcm[:n] * 1.0 + Xcm[n:] * -0.5 - y
+        q = orc.Q(B, F, r, r, nn, lu, threads=threads)
+    ll = -0.5 * (ld + q)
+    return (ll, B, F) if keep else ll
+
+
+def cpu_reference_impl():
+    """The CPU implementation the reference arm and cpu_baseline time: the reference's own
+    src/*.cpp compiled through the R-API stand-in (oracle/_ref) where that build exists -- it
+    is compiled from the spNNGP sources, which only the build host has -- else the oracle's C
+    port of the same routines (bit-identical results to the reference build at this workload;
+    the same speed on the build host)."""
+    from oracle.oracle import Oracle, Reference, build
+
+    build()
+    try:
+        return Reference(), "reference", "the reference's own src/rNNGP.cpp updateBF and src/util.cpp Q " \
+                                         "(compiled unmodified against an R-API stand-in)"
+    except Exception as e:
+        why = f"reference build not present on this host ({type(e).__name__})"
+        return Oracle(), "port", f"the oracle's C port of src/rNNGP.cpp:46-101 and src/util.cpp:261-280; {why}"
 
 
 def nngp_draw(sp, ctx, c, nn, lu, m, model, theta, rng):
@@ -291,6 +326,39 @@ def section_mcmc_batch(sp, ctx, dev, iters, n_inst=256, seed=77):
     }
 
 
+def section_parity(sp, ctx, c, nbr, ll_cpu, B_cpu, F_cpu, ll64, ll32, threads, kind):
+    """Parity at the headline workload itself (n = 1e6, m = 15) against the CPU implementation:
+    the oracle's code-book neighbor search compared bit for bit with the GPU's lists and
+    distances, the CPU log-likelihood against the GPU's FP64 and FP32R fused passes, and the
+    CPU B and F against the GPU's FP64 and FP32R updateBF (host-pointer entry point)."""
+    from oracle.oracle import Oracle
+
+    ccm = np.ascontiguousarray(c.T).reshape(-1)
+    t0 = time.perf_counter()
+    nn_o, d_o, lu_o = Oracle().mkNNIndxCB(ccm, M, threads=threads)
+    knn_cpu_s = time.perf_counter() - t0
+    out = {"n": N, "m": M, "checked_against": kind,
+           "nn_bitexact": bool(np.array_equal(nn_o, nbr["nnIndx"]) and np.array_equal(lu_o, nbr["nnIndxLU"])),
+           "nn_dist_bitexact": bool(np.array_equal(d_o, nbr["nnDist"])),
+           "oracle_knn_seconds": knn_cpu_s,
+           "loglik_cpu": ll_cpu,
+           "fp64_loglik_rel_err_vs_cpu": abs(ll64 - ll_cpu) / abs(ll_cpu),
+           "fp32r_loglik_rel_err_vs_cpu": abs(ll32 - ll_cpu) / abs(ll_cpu)}
+    scale = max(1.0, float(np.max(np.abs(B_cpu))))
+    for prec in ("fp64", "fp32r"):
+        B, F, _ = sp.updateBF(c, nbr["nnIndx"], nbr["nnIndxLU"], M, COV, THETA, prec, ctx=ctx)
+        out[f"{prec}_B_max_err_rel_max_abs_vs_cpu"] = float(np.max(np.abs(B - B_cpu)) / scale)
+        out[f"{prec}_F_max_rel_err_vs_cpu"] = float(np.max(np.abs(F - F_cpu) / F_cpu))
+        del B, F
+    out["fp64_within_1e-10"] = bool(out["fp64_loglik_rel_err_vs_cpu"] <= 1e-10 and
+                                    out["fp64_B_max_err_rel_max_abs_vs_cpu"] <= 1e-10 and
+                                    out["fp64_F_max_rel_err_vs_cpu"] <= 1e-10)
+    out["fp32r_within_1e-6"] = bool(out["fp32r_loglik_rel_err_vs_cpu"] <= 1e-6 and
+                                    out["fp32r_B_max_err_rel_max_abs_vs_cpu"] <= 1e-6 and
+                                    out["fp32r_F_max_rel_err_vs_cpu"] <= 1e-6)
+    return out
+
+
 # Config-1 models at effective ranges 0.05 and 0.5 (the distance where the correlation falls to
 # 0.05): exponential phi = 2.9957 / range, Matern nu = 1.5 phi = 4.7439 / range, gaussian
 # phi = 1.7308 / range with a 1e-6 nugget (the ill-conditioned case).
@@ -375,6 +443,97 @@ def section_accuracy(sp, ctx, dev, n=N, ms=(15, 32), seed=2024, reps=3):
             "note": "pass_ms: the whole fused likelihood pass timed with CUDA events on the launching stream "
                     f"(mean of {reps}); fp32r_primary_kernel_ms: its FP32R kernel alone; the gaussian cases "
                     "(1e-6 nugget) are too ill-conditioned for a float factor and run almost entirely in FP64"}
+
+
+def section_config0(sp, ctx, skip_cpu=False):
+    """The plain response model at its CPU-sized configuration (n = 2000, m = 15, exponential,
+    2000 samples; inputs, host-fed streams and the reference's own chain from
+    tests/golden/config0_golden.npz): MCMC iterations/s of the GPU chain (FP64 and FP32R,
+    through the public rNNGP call with host data) against the CPU implementation on all host
+    cores with the same streams, and whether each chain moves at the reference's iterations."""
+    from oracle.oracle import Oracle, build
+
+    g = np.load(os.path.join(HERE, "tests", "golden", "config0_golden.npz"))
+    nS = g["theta"].shape[1]
+    args = (g["y"], g["X"], 15, g["coords"], "exponential", g["nnIndx"], g["lu"], [2, 1], [2, 0.1], [3, 30], None,
+            [1.0, -0.5], g["theta_start"], g["tuning"], nS, g["normals"], g["unifs"])
+    gmoved = np.any(np.diff(g["theta"], axis=1) != 0, axis=0)
+    out = {"workload": "n=2000 uniform, X=[1,N(0,1)], w from a dense exponential GP (sigma2=1, phi=6), tau2=0.1, "
+                       "m=15, priors sigma.sq IG(2,1) tau.sq IG(2,0.1) phi U(3,30), 2000 samples, host-fed streams",
+           "samples": int(nS)}
+    for prec in ("fp64", "fp32r"):
+        sp.rNNGP(*args[:14], 50, *args[15:], precision=prec, ctx=ctx)  # warm-up: plan, graph capture
+        t0 = time.perf_counter()
+        r = sp.rNNGP(*args, precision=prec, ctx=ctx)
+        dt = time.perf_counter() - t0
+        moved = np.any(np.diff(r["p.theta.samples"], axis=1) != 0, axis=0)
+        out[prec] = {"seconds": dt, "iterations_per_s": nS / dt,
+                     "same_decisions_as_reference": float(np.mean(moved == gmoved)),
+                     "theta_max_rel_err_vs_reference": float(np.max(np.abs(r["p.theta.samples"] - g["theta"]) /
+                                                                    np.abs(g["theta"])))}
+    if not skip_cpu:
+        build()
+        orc = Oracle()
+        thr = os.cpu_count() or 1
+        ccm = lambda a: np.ascontiguousarray(np.asarray(a).T).reshape(-1)  # noqa: E731
+        t0 = time.perf_counter()
+        ro = orc.rNNGP(g["y"], ccm(g["X"]), 15, ccm(g["coords"]), 0, g["nnIndx"], g["lu"], [2, 1], [2, 0.1], [3, 30],
+                       [0.5, 2.5], [1.0, -0.5], g["theta_start"], g["tuning"], nS, g["normals"], g["unifs"],
+                       threads=thr)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": nS / dt, "unit": "iterations/s", "cores": thr, "kind": "port",
+                               "identical_chain_to_reference": bool(np.array_equal(ro["theta"], g["theta"])),
+                               "sample": "the oracle's C port of rNNGP (src/rNNGP.cpp:103-421), the full 2000 "
+                                         "samples, OpenMP over locations"}
+        out["gpu_fp64_over_cpu"] = out["fp64"]["iterations_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
+def section_replicate(sp, ctx, n=N, n_samples=100, skip_cpu=False, seed=404):
+    """Replicated data (rNNGPReplicated, the y_rep of fit.rep / fitted.NNGP) at n = 1e6, m = 15,
+    exponential, n_samples parameter sets scattered around the headline theta: the
+    level-scheduled GPU solve through the public call (host data in and out), FP32R and FP64,
+    against the oracle's sequential recurrence on a two-sample slice of the same inputs."""
+    rng = np.random.default_rng(seed)
+    c, X, _ = workload(n)
+    nb = sp.mkNNIndxCB(c, M, ctx=ctx)
+    nn, lu = nb["nnIndx"], nb["nnIndxLU"]
+    th = np.array(THETA)[:, None] * rng.uniform(0.8, 1.25, size=(3, n_samples))
+    beta = rng.normal(size=(n_samples, 2))
+    z = rng.standard_normal(size=n * n_samples)
+    out = {"workload": f"n={n} uniform x-ordered, m={M}, exponential, {n_samples} samples (theta within x0.8-1.25 "
+                       f"of sigma2={THETA[0]} tau2={THETA[1]} phi={THETA[2]}), X=[1,N(0,1)]",
+           "samples": n_samples}
+    res = {}
+    for prec in ("fp32r", "fp64"):
+        sp.rNNGPReplicated(X, M, c, COV, nn, lu, beta[:2], th[:, :2], z[: 2 * n], precision=prec, ctx=ctx)  # warm
+        t0 = time.perf_counter()
+        r = sp.rNNGPReplicated(X, M, c, COV, nn, lu, beta, th, z, precision=prec, ctx=ctx)["y.rep.samples"]
+        dt = time.perf_counter() - t0
+        res[prec] = r[:, :2].copy()
+        out[prec] = {"seconds": dt, "samples_per_s": n_samples / dt, "solves_per_s": n * n_samples / dt,
+                     "h2d_bytes": int(z.nbytes + X.nbytes + c.nbytes + nn.nbytes + lu.nbytes),
+                     "d2h_bytes": int(8 * n * n_samples)}
+        del r
+    if not skip_cpu:
+        from oracle.oracle import Oracle, build
+
+        build()
+        thr = os.cpu_count() or 1
+        ccm = np.ascontiguousarray(c.T).reshape(-1)
+        Xcm = np.ascontiguousarray(X.T).reshape(-1)
+        t0 = time.perf_counter()
+        yo, st = Oracle().rNNGPReplicated(Xcm, M, ccm, 0, nn, lu, beta[:2], np.ascontiguousarray(th[:, :2].T).reshape(-1),
+                                          z[: 2 * n], threads=thr)
+        dt = time.perf_counter() - t0
+        scale = max(1.0, float(np.max(np.abs(yo))))
+        out["cpu_baseline"] = {"value": 2 / dt, "unit": "samples/s", "cores": thr, "kind": "port",
+                               "sample": "the oracle's C port of rNNGPReplicated (src/rNNGPReplicated.cpp:183-205: "
+                                         "updateBF with OpenMP, then the sequential recurrence) on the first 2 samples"}
+        out["fp64_max_err_vs_cpu"] = float(np.max(np.abs(res["fp64"] - yo)) / scale)
+        out["fp32r_max_err_vs_cpu"] = float(np.max(np.abs(res["fp32r"] - yo)) / scale)
+        out["gpu_fp32r_over_cpu"] = out["fp32r"]["samples_per_s"] / out["cpu_baseline"]["value"]
+    return out
 
 
 def clustered_coords(rng, n, blobs=20, sd=0.03, uniform_frac=0.2):
@@ -525,30 +684,28 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from oracle.oracle import Oracle, build
+    from oracle.oracle import Oracle
 
-    build()
-    orc = Oracle()
+    impl, kind, what = cpu_reference_impl()
     threads = os.cpu_count() or 1
     c, X, y = workload()
     ccm = np.ascontiguousarray(c.T).reshape(-1)
     Xcm = np.ascontiguousarray(X.T).reshape(-1)
-    nn, _, lu = orc.mkNNIndxCB(ccm, M, threads=threads)
+    nn, _, lu = Oracle().mkNNIndxCB(ccm, M, threads=threads)  # neighbor search outside the timed step
     for _ in range(args.warmup):
-        cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, N)
+        cpu_step_oracle(impl, ccm, nn, lu, Xcm, y, threads, N)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, N)
+        cpu_step_oracle(impl, ccm, nn, lu, Xcm, y, threads, N)
     dt = (time.perf_counter() - t0) / max(args.steps, 1)
     value = N / dt
-    sample = f"full workload: updateBF + Q over all n={N} locations per step, {threads} OpenMP threads"
+    sample = f"full workload: updateBF + Q over all n={N} locations per step, {threads} OpenMP threads; {what}"
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"n={N} uniform, m={M}, {COV} theta={THETA}, updateBF+loglik",
-                   "l2": "host path"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "config": bench_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -694,29 +851,31 @@ def run_ours(args):
     tune = ctx.autotune_report()
 
     cpu = None
+    parity = None
     if rank == 0 and not args.skip_cpu:
         try:
-            from oracle.oracle import Oracle, build
-
-            build()
-            orc = Oracle()
+            impl, kind, what = cpu_reference_impl()
             threads = os.cpu_count() or 1
             Xcm = np.ascontiguousarray(X.T).reshape(-1)
-            cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, N)
+            ll_cpu, B_cpu, F_cpu = cpu_step_oracle(impl, ccm, nn, lu, Xcm, y, threads, N, keep=True)
             t0 = time.perf_counter()
             reps = 2
             for _ in range(reps):
-                cpu_step_oracle(orc, ccm, nn, lu, Xcm, y, threads, N)
+                cpu_step_oracle(impl, ccm, nn, lu, Xcm, y, threads, N)
             cdt = (time.perf_counter() - t0) / reps
-            cpu = {"value": N / cdt, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"updateBF + Q over all n={N} locations (the oracle's C port of src/rNNGP.cpp:46-101 "
-                             f"and src/util.cpp:261-280), mean of {reps} runs"}
+            cpu = {"value": N / cdt, "unit": UNIT, "cores": threads, "kind": kind,
+                   "sample": f"updateBF + Q over all n={N} locations ({what}), mean of {reps} runs"}
+            parity = section_parity(sp, ctx, c, nbr, ll_cpu, B_cpu, F_cpu, ll64, ll32, threads, kind)
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
 
     sections = {}
     if rank == 0 and args.sections:
         clk2 = ClockSampler(dev.index).__enter__()
+        if "config0" in args.sections:
+            sections["config0_mcmc"] = section_config0(sp, ctx, args.skip_cpu)
+        if "rep" in args.sections:
+            sections["replicate"] = section_replicate(sp, ctx, skip_cpu=args.skip_cpu)
         if "accuracy" in args.sections:
             sections["accuracy"] = section_accuracy(sp, ctx, dev)
         if "mcmc" in args.sections:
@@ -739,10 +898,9 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": max_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": f"n={N} uniform [0,1]^2 x-ordered, m={M} code-book neighbors, {COV} "
-                                   f"sigma2={THETA[0]} tau2={THETA[1]} phi={THETA[2]}, fused updateBF+loglik, "
-                                   f"X=[1,N(0,1)], FP32 build/Cholesky + one double-float (Dot2) residual refinement",
-                       "l2": "flushed between timed steps (512 MB write); inputs ~100 MB"},
+            "config": bench_config(),
+            "form": "FP32 covariance build and Cholesky, one double-float (Dot2) residual refinement; "
+                    "FP64 re-solve of the locations the error estimate flags",
             "fp64_form": {"value": N / (ms64 * 1e-3), "ms_per_step": ms64, "kernel_ms": kms64},
             "fp32r_over_fp64": ms64 / ms32,
             "loglik_rel_err_fp32r_vs_fp64": abs(ll32 - ll64) / abs(ll64),
@@ -765,6 +923,7 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
+            "parity": parity,
         }
         out.update(sections)
         print(json.dumps(out), flush=True)
@@ -826,9 +985,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--sections", default="accuracy,mcmc,conj,serve",
-                    help="comma-separated extra workloads reported beside the headline (accuracy, mcmc, conj, "
-                         "serve), or ''")
+    ap.add_argument("--sections", default="config0,rep,accuracy,mcmc,conj,serve",
+                    help="comma-separated extra workloads reported beside the headline (config0, rep, accuracy, "
+                         "mcmc, conj, serve), or ''")
     ap.add_argument("--mcmc-iters", type=int, default=200)
     ap.add_argument("--launch-shape", default="",
                     help="W,G[,T]: run the FP32R register kernel with W warps per block, grid mode G and "

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <vector>
 #include "nngp_internal.h"
+#include "nngp_rep.h"
 #include "nngp_pred.h"
 #include "nngp_small.cuh"
 
@@ -77,32 +78,6 @@ __global__ void conj_fit_kernel(const double *__restrict__ out, int ng, int g, i
     bb[(size_t)k * p + i] = v[i];
   }
   for (int i = 0; i < p * p; i++) bBInv[(size_t)k * p * p + i] = V[i];
-}
-
-// v_i = B_i v_N(i) + sqrt(F_i) z_i, then y_rep = v + X beta_s; one thread per sample.
-__global__ void replicate_kernel(int ns, int n, int p, const double *__restrict__ B, int64_t nI,
-                                 const double *__restrict__ F, const int *__restrict__ nnIndx,
-                                 const int *__restrict__ nnLU, const double *__restrict__ z,
-                                 const double *__restrict__ X, const double *__restrict__ beta, int nSamples,
-                                 int s0, double *__restrict__ yRep) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ns) return;
-  const int s = s0 + t;
-  const double *Bs = B + (size_t)t * nI;
-  const double *Fs = F + (size_t)t * n;
-  const double *zs = z + (size_t)s * n;
-  double *out = yRep + (size_t)s * n;
-  for (int i = 0; i < n; i++) {
-    const int off = nnLU[i], cnt = nnLU[n + i];
-    double acc = 0.0;
-    for (int j = 0; j < cnt; j++) acc += Bs[off + j] * out[nnIndx[off + j]];
-    out[i] = acc + sqrt(Fs[i]) * zs[i];
-  }
-  for (int i = 0; i < n; i++) {
-    double xb = 0.0;
-    for (int j = 0; j < p; j++) xb += X[(size_t)j * n + i] * beta[s + (size_t)nSamples * j];
-    out[i] += xb;
-  }
 }
 
 // Batched form of conj_fit_kernel: evaluation e belongs to a dataset of size ns[e].
@@ -409,43 +384,36 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
   }
   CovParams *dth = (CovParams *)T.up(th.data(), sizeof(CovParams) * nSamples);
   unsigned long long *dst = (unsigned long long *)T.up(nullptr, sizeof(unsigned long long));
-  // samples per chunk: keep the chunk's B arrays near 2 GB
-  const size_t perB = sizeof(double) * (size_t)((nI > 0 ? nI : 1) + n);
-  int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nSamples, ((size_t)2 << 30) / perB));
-  double *dB = (double *)T.up(nullptr, sizeof(double) * (size_t)(nI > 0 ? nI : 1) * chunk);
-  double *dF = (double *)T.up(nullptr, sizeof(double) * (size_t)n * chunk);
-  double *out = (double *)T.up(nullptr, sizeof(double) * 2 * (size_t)chunk);
+  std::vector<long long> zoff(nSamples);
+  for (int s = 0; s < nSamples; s++) zoff[s] = (long long)s * n;
+  const long long *dzoff = (const long long *)T.up(zoff.data(), sizeof(long long) * nSamples);
   if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
   nngp_prepare_coords(ctx, dcm, n, xy, xyf);
   int st = nngp_reset_status(ctx, dst);
-  for (int s0 = 0; !st && s0 < nSamples; s0 += chunk) {
-    const int ns = std::min(chunk, nSamples - s0);
-    std::vector<BFData> datas(ns);
-    std::vector<PassEval> ev(ns);
-    for (int t = 0; t < ns; t++) {
-      BFData d{};
-      d.n = n;
-      d.m = m;
-      d.xy = xy;
-      d.xyf = xyf;
-      d.nnIndx = dnn;
-      d.nnLU = dlu;
-      d.B = dB + (size_t)t * (nI > 0 ? nI : 1);
-      d.F = dF + (size_t)t * n;
-      datas[t] = d;
-      ev[t] = PassEval{t, s0 + t};
-    }
-    BFPlan plan;
-    st = nngp_bf_plan(ctx, &plan, precision, 0, 0, datas, dth, ev, dst, nngp_plan_cov(th.data(), nSamples));
-    if (!st) st = nngp_bf_run(ctx, &plan, out);
-    if (!st) {
-      replicate_kernel<<<nb(ns, 32), 32, 0, ctx->stream>>>(ns, n, p, dB, nI > 0 ? nI : 1, dF, dnn, dlu, dz, dX,
-                                                            dbeta, nSamples, s0, dy);
-      ctx->launches++;
-    }
-    nngp_bf_plan_free(ctx, &plan);
-  }
   if (st) return st;
+  // the level-scheduled solve of every sample's recurrence (nngp_rep.cu)
+  RepSpec rs{};
+  rs.n = n;
+  rs.m = m;
+  rs.p = p;
+  rs.nRep = nSamples;
+  rs.precision = precision;
+  rs.cov = nngp_plan_cov(th.data(), nSamples);
+  rs.xb_first = 0;  // v, then + beta_j X_j in order (src/rNNGPReplicated.cpp:204 dgemv)
+  rs.xy = xy;
+  rs.xyf = xyf;
+  rs.nnIndx = dnn;
+  rs.nnLU = dlu;
+  rs.X = dX;
+  rs.d_theta = dth;
+  rs.beta = dbeta;
+  rs.bs_r = 1;
+  rs.bs_j = nSamples;
+  rs.z = dz;
+  rs.d_zoff = dzoff;
+  rs.yRep = dy;
+  rs.d_status = dst;
+  if ((st = nngp_replicate_solve(ctx, rs))) return st;
   if ((st = nngp_check_status(ctx, dst, "rNNGPReplicated"))) return st;
   NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(yRep, dy, sizeof(double) * (size_t)n * nSamples, cudaMemcpyDeviceToHost, ctx->stream));
   NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

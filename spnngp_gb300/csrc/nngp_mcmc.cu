@@ -15,15 +15,19 @@
 // (src/rNNGP.cpp:306); that recomputation is deterministic, so the current
 // theta's log-determinant and Gram are cached instead, which halves the solves
 // without changing any value.  Q(X beta - y) comes from the Gram:
-// beta'Gxx beta - 2 beta'Gxy + Gyy.  Iterations with a replicate draw
-// (fit.rep) additionally run the standalone B/F pass at the current theta and
-// the sequential recurrence of src/rNNGP.cpp:24-42.
+// beta'Gxx beta - 2 beta'Gxy + Gyy.  An iteration with a replicate draw
+// (fit.rep, src/rNNGP.cpp:300-303,309-313) records the current theta, the beta
+// draw and where its n normals start in the stream; the draws do not feed back
+// into the chain, so after the last iteration all of them are made at once by
+// the level-scheduled solve of nngp_rep.cu (the recurrence of
+// src/rNNGP.cpp:24-42 for every recorded theta).
 // Random numbers come from host-fed streams in the reference's order.  Each
 // iteration is captured once as a CUDA graph and replayed.
 #include <cuda_runtime.h>
 #include <cmath>
 #include <vector>
 #include "nngp_internal.h"
+#include "nngp_rep.h"
 #include "nngp_small.cuh"
 
 namespace {
@@ -42,9 +46,10 @@ struct MCConst {
   double *thetaOut;    // nTheta x nSamples
   double *repOut;      // n x nRep
   const double *X;     // n x p column-major
-  const double *B;     // standalone pass outputs (replicates)
-  const double *F;
-  const int *nnIndx, *nnLU;
+  // replicate records, one per draw: the current theta, the beta draw, the normals' offset
+  CovParams *repTheta;
+  double *repBeta;     // nRep x p
+  long long *repZoff;
   const double *out;   // this instance's (log F, Gram) sums in its size class's output buffer
 };
 
@@ -161,11 +166,16 @@ __global__ void mc_pre_kernel(const MCConst *__restrict__ cs, MCState *__restric
     for (int j = 0; j <= i; j++) s += st.L[j * p + i] * z[j];
     st.beta[i] = s;
   }
-  // replicate draw at the current theta consumes n normals here
+  // replicate draw at the current theta consumes n normals here; it is recorded and made
+  // after the chain
   st.doRep = (c.repIndx && c.repIndx[st.s]) ? 1 : 0;
   if (st.doRep) {
     st.repStart = st.npos;
     if (st.npos + c.n > c.nNormals) st.status = 3;
+    set_params(c.repTheta[st.repCnt], c.model, st.theta);
+    for (int i = 0; i < p; i++) c.repBeta[(size_t)st.repCnt * p + i] = st.beta[i];
+    c.repZoff[st.repCnt] = st.npos;
+    st.repCnt++;
     st.npos += c.n;
   }
   const double q = quad_from_gram(st.G, p, st.beta);
@@ -205,32 +215,6 @@ __global__ void mc_post_kernel(const MCConst *__restrict__ cs, MCState *__restri
   for (int i = 0; i < p; i++) c.betaOut[(size_t)st.s * p + i] = st.beta[i];
   for (int t = 0; t < c.nTheta; t++) c.thetaOut[(size_t)st.s * c.nTheta + t] = st.theta[t];
   st.s++;
-}
-
-// Replicate: v_i = B_i v_N(i) + sqrt(F_i) z_i sequentially, y_rep = X beta + v.
-__global__ void mc_rep_kernel(const MCConst *__restrict__ cs, MCState *__restrict__ sts, int ninst) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ninst) return;
-  const MCConst &c = cs[k];
-  MCState &st = sts[k];
-  if (st.status || !st.doRep) return;
-  double *out = c.repOut + (size_t)st.repCnt * c.n;
-  const double *z = c.normals + st.repStart;
-  const int n = c.n;
-  for (int i = 0; i < n; i++) {
-    double v = sqrt(c.F[i]) * z[i];
-    const int off = c.nnLU[i], cnt = c.nnLU[n + i];
-    double s = 0.0;
-    for (int j = 0; j < cnt; j++) s += c.B[off + j] * out[c.nnIndx[off + j]];
-    out[i] = (i == 0) ? v : s + v;
-  }
-  // the recurrence read out[] as v; now add X beta
-  for (int i = 0; i < n; i++) {
-    double xb = 0.0;
-    for (int j = 0; j < c.p; j++) xb += c.X[(size_t)j * n + i] * st.beta[j];
-    out[i] += xb;
-  }
-  st.repCnt++;
 }
 
 __global__ void build_v_kernel(const double *__restrict__ X, const double *__restrict__ y, int n, int p,
@@ -308,11 +292,6 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     d.nnIndx = I.nnIndx;
     d.nnLU = I.nnLU;
     d.V = V;
-    if (anyRep) {
-      const int64_t nI = nngp_nindx(I.n, I.m);
-      d.B = (double *)own(sizeof(double) * (nI > 0 ? nI : 1));
-      d.F = (double *)own(sizeof(double) * I.n);
-    }
     datas[k] = d;
     MCConst &c = consts[k];
     c = MCConst{};
@@ -337,10 +316,17 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     c.thetaOut = I.thetaOut;
     c.repOut = I.repOut;
     c.X = I.X;
-    c.B = d.B;
-    c.F = d.F;
-    c.nnIndx = I.nnIndx;
-    c.nnLU = I.nnLU;
+    if (anyRep && I.repIndx) {
+      int nrep = 0;
+      for (int v : *host_rep) nrep += v != 0;
+      c.repTheta = (CovParams *)own(sizeof(CovParams) * (nrep > 0 ? nrep : 1));
+      c.repBeta = (double *)own(sizeof(double) * (size_t)(nrep > 0 ? nrep : 1) * p);
+      c.repZoff = (long long *)own(sizeof(long long) * (nrep > 0 ? nrep : 1));
+      if (!c.repTheta || !c.repBeta || !c.repZoff) {
+        release();
+        return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+      }
+    }
     MCState &s = states[k];
     s = MCState{};
     for (int t = 0; t < 4; t++) s.theta[t] = s.cand[t] = I.thetaStart[t];
@@ -368,7 +354,7 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
   };
   std::vector<int> cls(ninst), pos(ninst);
   std::vector<std::vector<BFData>> cdatas(NCLS);
-  std::vector<std::vector<PassEval>> cevCand(NCLS), cevCur(NCLS);
+  std::vector<std::vector<PassEval>> cevCand(NCLS);
   for (int k = 0; k < ninst; k++) {
     const MCInstance &I = insts[k];
     const bool gen = I.model == 2 && (I.tuning[3] != 0.0 || th[2 * k].halfk < 0);
@@ -377,15 +363,13 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     pos[k] = (int)cdatas[cls[k]].size();
     cdatas[cls[k]].push_back(datas[k]);
     cevCand[cls[k]].push_back(PassEval{pos[k], 2 * k + 1});
-    cevCur[cls[k]].push_back(PassEval{pos[k], 2 * k});
   }
-  double *d_outc[NCLS] = {}, *d_out0c[NCLS] = {};
+  double *d_outc[NCLS] = {};
   for (int c = 0; c < NCLS; c++) {
     const size_t cnt = cdatas[c].size();
     if (!cnt) continue;
     d_outc[c] = (double *)own(sizeof(double) * 2 * cnt * ng);
-    d_out0c[c] = (double *)own(sizeof(double) * 2 * cnt);
-    if (!d_outc[c] || !d_out0c[c]) {
+    if (!d_outc[c]) {
       release();
       return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
     }
@@ -415,23 +399,17 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     release();
     return st;
   }
-  BFPlan planCand[NCLS], planCur[NCLS];
-  bool haveCand[NCLS] = {}, haveCur[NCLS] = {};
+  BFPlan planCand[NCLS];
+  bool haveCand[NCLS] = {};
   auto free_plans = [&]() {
-    for (int c = 0; c < NCLS; c++) {
+    for (int c = 0; c < NCLS; c++)
       if (haveCand[c]) nngp_bf_plan_free(ctx, &planCand[c]);
-      if (haveCur[c]) nngp_bf_plan_free(ctx, &planCur[c]);
-    }
   };
   for (int c = 0; c < NCLS && !st; c++) {
     if (cdatas[c].empty()) continue;
     const int cov = c % 5;
     st = nngp_bf_plan(ctx, &planCand[c], precision, 1, nv, cdatas[c], d_th, cevCand[c], d_status, cov);
     haveCand[c] = true;
-    if (!st && anyRep) {
-      st = nngp_bf_plan(ctx, &planCur[c], precision, 0, 0, cdatas[c], d_th, cevCur[c], d_status, cov);
-      haveCur[c] = true;
-    }
   }
   if (st) {
     free_plans();
@@ -452,7 +430,7 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     mc_init_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
     ctx->launches++;
   }
-  // one iteration as a graph (with and without the replicate draw).  The classes' passes are
+  // one iteration as a graph.  The classes' passes are
   // independent: each class runs on its own branch (side streams forked from and joined back
   // to the capturing stream), so small classes overlap instead of queueing.
   int nclasses = 0;
@@ -491,17 +469,13 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     }
     return r;
   };
-  auto capture = [&](bool rep, cudaGraphExec_t *exec) -> int {
+  auto capture = [&](cudaGraphExec_t *exec) -> int {
     cudaGraph_t g;
     const cudaError_t eb = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
     if (eb != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(eb));
     int s2 = NNGP_OK;
     mc_pre_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
-    if (rep) {
-      s2 = fan_out([&](int c) { return haveCur[c] ? nngp_bf_run(ctx, &planCur[c], d_out0c[c]) : NNGP_OK; });
-      mc_rep_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, ninst);
-    }
-    if (!s2) s2 = fan_out([&](int c) { return nngp_bf_run(ctx, &planCand[c], d_outc[c]); });
+    s2 = fan_out([&](int c) { return nngp_bf_run(ctx, &planCand[c], d_outc[c]); });
     mc_post_kernel<<<nblk(ninst, 64), 64, 0, ctx->stream>>>(d_c, d_s, d_th, ninst);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (s2) return s2;
@@ -511,25 +485,18 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
     if (e != cudaSuccess) return nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     return NNGP_OK;
   };
-  cudaGraphExec_t gPlain = nullptr, gRep = nullptr;
+  cudaGraphExec_t gPlain = nullptr;
   const bool timing = ctx->timing;
   ctx->timing = false;  // no per-pass events inside a captured graph
   const int64_t launches_before = ctx->launches;
-  if (!st) st = capture(false, &gPlain);
+  if (!st) st = capture(&gPlain);
   const int64_t per_plain = ctx->launches - launches_before;
-  int64_t per_rep = 0;
-  if (!st && anyRep) {
-    const int64_t b = ctx->launches;
-    st = capture(true, &gRep);
-    per_rep = ctx->launches - b;
-  }
   ctx->launches = launches_before;  // captured launches are counted when replayed below
   ctx->timing = timing;
   for (int s = 0; !st && s < nS; s++) {
-    const bool rep = anyRep && (*host_rep)[s] != 0;
-    cudaError_t e = cudaGraphLaunch(rep ? gRep : gPlain, ctx->stream);
+    cudaError_t e = cudaGraphLaunch(gPlain, ctx->stream);
     if (e != cudaSuccess) st = nngp_fail(ctx, NNGP_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
-    ctx->launches += rep ? per_rep : per_plain;
+    ctx->launches += per_plain;
   }
   if (!st) {
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -541,7 +508,6 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
   for (int c = 0; c < NCLS; c++)
     if (evJoin[c]) cudaEventDestroy(evJoin[c]);
   if (gPlain) cudaGraphExecDestroy(gPlain);
-  if (gRep) cudaGraphExecDestroy(gRep);
   if (!st) st = nngp_check_status(ctx, d_status, "rNNGP");
   if (!st) {
     MC_TRY(cudaMemcpy(states.data(), d_s, sizeof(MCState) * ninst, cudaMemcpyDeviceToHost));
@@ -550,6 +516,35 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
       if (states[k].status == 2) st = nngp_fail(ctx, NNGP_ERR_NOT_SPD, "rNNGP: beta Gram matrix not positive definite (dpotrf failed)");
       if (states[k].status == 3) st = nngp_fail(ctx, NNGP_ERR_STREAM, "rNNGP: a host-fed random stream ran out");
     }
+  }
+  // the recorded replicate draws, every one of an instance in one level-scheduled solve
+  for (int k = 0; k < ninst && !st; k++) {
+    const MCConst &c = consts[k];
+    if (!c.repTheta || states[k].repCnt == 0) continue;
+    RepSpec rs{};
+    rs.n = c.n;
+    rs.m = insts[k].m;
+    rs.p = p;
+    rs.nRep = states[k].repCnt;
+    rs.precision = precision;
+    rs.cov = cls[k] % 5;
+    rs.xb_first = 1;  // X beta (dgemv), then + v (daxpy): src/rNNGP.cpp:300-303,311
+    rs.xy = datas[k].xy;
+    rs.xyf = datas[k].xyf;
+    rs.nnIndx = insts[k].nnIndx;
+    rs.nnLU = insts[k].nnLU;
+    rs.X = insts[k].X;
+    rs.d_theta = c.repTheta;
+    rs.beta = c.repBeta;
+    rs.bs_r = p;
+    rs.bs_j = 1;
+    rs.z = c.normals;
+    rs.d_zoff = c.repZoff;
+    rs.yRep = c.repOut;
+    rs.d_status = d_status;
+    if ((st = nngp_reset_status(ctx, d_status))) break;
+    st = nngp_replicate_solve(ctx, rs);
+    if (!st) st = nngp_check_status(ctx, d_status, "rNNGP replicates");
   }
   free_plans();
   release();

@@ -2,8 +2,12 @@
 C++ (src/*.cpp of spNNGP 1.0.1, compiled unmodified against the R-API stand-in
 by oracle/Makefile -> oracle/_ref/libspnngp_ref.so).
 
-Run here, where the reference sources are mounted:
-    python tests/golden/make_golden.py [/path/to/spNNGP]
+Run where the reference sources are available (the spNNGP source tree, given
+as the argument or in the SPNNGP_REFERENCE environment variable):
+    python tests/golden/make_golden.py /path/to/spNNGP
+It writes reference_golden.npz (small cases of every routine) and
+config0_golden.npz (the n = 2000, m = 15 response model with a 2000-sample
+chain).
 The inputs are seeded synthetic data (uniform coordinates, a regular lattice
 with exact distance ties, coordinates with repeated x values); the random
 streams fed to the MCMC are stored with the outputs so a run can be replayed.
@@ -138,7 +142,40 @@ def main(ref_root):
     path = os.path.join(HERE, "reference_golden.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
+    config0(R)
+
+
+def config0(R):
+    """The plain response model at its CPU-sized configuration: n = 2000 locations iid
+    U[0,1]^2 in x order, X = [1, N(0,1)], beta = (1, -0.5), w from the full exponential GP
+    (sigma^2 = 1, phi = 6) by a dense Cholesky factor, y = X beta + w + N(0, 0.1); m = 15
+    code-book neighbors; priors sigma.sq IG(2, 1), tau.sq IG(2, 0.1), phi U(3, 30); 2000
+    samples from theta = (1, 0.1, 6) with tuning (0.1, 0.1, 0.5).  Stores the inputs, the
+    host-fed streams and the reference's chain."""
+    rng = np.random.default_rng(20250601)
+    n, m, p, nS = 2000, 15, 2, 2000
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    D = np.sqrt(((c[:, None, :] - c[None, :, :]) ** 2).sum(-1))
+    w = np.linalg.cholesky(np.exp(-6.0 * D) + 1e-10 * np.eye(n)) @ rng.normal(size=n)
+    y = X @ np.array([1.0, -0.5]) + w + rng.normal(scale=np.sqrt(0.1), size=n)
+    a = R.mkNNIndxCB(cm(c), m)
+    assert a[3] == 0, R.error()
+    ts, tu = [1.0, 0.1, 6.0], [0.1, 0.1, 0.5]
+    normals = rng.normal(size=nS * (p + len(ts)) + 16)
+    unifs = rng.uniform(size=nS + 4)
+    r = R.rNNGP(y, cm(X), m, cm(c), 0, a[0], a[2], [2, 1], [2, 0.1], [3, 30], [0.5, 2.5], [1.0, -0.5], ts, tu, nS,
+                normals, unifs)
+    assert r["status"] == 0, R.error()
+    out = dict(coords=c, X=X, y=y, nnIndx=a[0], nnDist=a[1], lu=a[2], theta_start=np.array(ts), tuning=np.array(tu),
+               normals=normals, unifs=unifs, beta=r["beta"], theta=r["theta"], used=np.array(r["used"][:2]))
+    path = os.path.join(HERE, "config0_golden.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes,", len(out), "arrays")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPNNGP_REFERENCE")
+    if not src:
+        sys.exit("usage: make_golden.py /path/to/spNNGP (or set SPNNGP_REFERENCE)")
+    main(src)

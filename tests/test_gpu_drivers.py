@@ -120,7 +120,65 @@ def test_rNNGPReplicated_matches_reference(sp, golden):
     g = golden
     r = sp.rNNGPReplicated(g["mc_X"], 10, g["mc_coords"], 0, g["mc_nnIndx"], g["mc_lu"], g["rp_beta"],
                            g["pr_theta"], g["rp_normals"])
-    assert np.max(np.abs(r["y.rep.samples"] - g["rp_yrep"])) <= 1e-8
+    assert np.max(np.abs(r["y.rep.samples"] - g["rp_yrep"])) <= 1e-9 * max(1.0, np.max(np.abs(g["rp_yrep"])))
+
+
+@pytest.mark.parametrize("model,theta", [(0, (1.0, 0.1, 6.0)), (2, (1.0, 0.2, 12.0, 1.5))])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32r", 1e-6)])
+def test_rNNGPReplicated_level_schedule_matches_oracle(sp, orc, model, theta, precision, tol):
+    """The level-scheduled solve (one launch per level of the neighbor DAG over every sample)
+    against the oracle's sequential recurrence at a size with ~1200 levels."""
+    rng = np.random.default_rng(71)
+    n, m, p, nS = 20000, 15, 2, 6
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    o = orc.mkNNIndxCB(cm(c), m)
+    nT = len(theta)
+    th = np.array(theta)[:, None] * rng.uniform(0.8, 1.25, size=(nT, nS))
+    beta = rng.normal(size=(nS, p))
+    z = rng.normal(size=n * nS)
+    r = sp.rNNGPReplicated(X, m, c, model, o[0], o[2], beta, th, z, precision=precision)
+    yo, st = orc.rNNGPReplicated(cm(X), m, cm(c), model, o[0], o[2], beta, cm(th), z)
+    assert st == 0
+    assert np.max(np.abs(r["y.rep.samples"] - yo)) <= tol * max(1.0, np.max(np.abs(yo)))
+
+
+def test_rNNGPReplicated_rejects_non_predecessor_neighbors(sp, orc):
+    """A neighbor list naming a later location is refused by the level schedule's own check."""
+    rng = np.random.default_rng(72)
+    n, m = 500, 10
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    o = orc.mkNNIndxCB(cm(c), m)
+    nn = o[0].copy()
+    lu = o[2]
+    nn[lu[300]] = 400  # location 300's first neighbor: a successor
+    with pytest.raises(sp.NNGPError) as e:
+        sp.rNNGPReplicated(X, m, c, 0, nn, lu, rng.normal(size=(2, 2)), np.array([[1.0, 1.0], [0.1, 0.1], [6.0, 6.0]]),
+                           rng.normal(size=2 * n))
+    assert e.value.status == 1
+
+
+def test_rNNGP_replicates_match_oracle_at_scale(sp, orc):
+    """fit.rep in the response MCMC: the recorded draws, made after the chain by the level
+    solve, against the oracle's in-chain sequential recurrence."""
+    rng = np.random.default_rng(73)
+    n, m, p, nS, nR = 6000, 15, 2, 40, 4
+    c = xorder(rng.uniform(size=(n, 2)))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    y = X @ [1.0, -0.5] + rng.normal(size=n)
+    o = orc.mkNNIndxCB(cm(c), m)
+    ri = np.zeros(nS, np.int32)
+    ri[[5, 17, 30, 39]] = 1
+    normals = rng.normal(size=nS * 5 + nR * n + 8)
+    unifs = rng.uniform(size=nS + 2)
+    args = (y, cm(X), m, cm(c), 0, o[0], o[2], [2, 1], [2, 0.1], [3, 30], [0, 0], [1.0, -0.5], [1.0, 0.2, 6.0],
+            [0.1, 0.1, 0.4], nS, normals, unifs)
+    ro = orc.rNNGP(*args, n_rep=nR, rep_indx=ri)
+    rg = sp.rNNGP(y, X, m, c, 0, o[0], o[2], [2, 1], [2, 0.1], [3, 30], None, [1.0, -0.5], [1.0, 0.2, 6.0],
+                  [0.1, 0.1, 0.4], nS, normals, unifs, n_rep=nR, rep_indx=ri)
+    assert rg["accept"] == ro["accept"]
+    assert np.max(np.abs(rg["y.rep.samples"] - ro["rep"])) <= 1e-9 * max(1.0, np.max(np.abs(ro["rep"])))
 
 
 def test_cNNGP_many_grid_points_match_oracle(sp, orc):
@@ -219,3 +277,65 @@ def test_rNNGP_batch_matches_oracle(sp, orc):
                        P["theta_starting"], P["tuning"], P["n_samples"], P["normals"], P["unifs"])
         assert r["accept"] == ro["accept"]
         assert np.max(np.abs(r["p.theta.samples"] - ro["theta"]) / ro["theta"]) <= TOL
+
+
+@pytest.fixture(scope="module")
+def config0():
+    import os
+
+    from conftest import ROOT
+
+    return np.load(os.path.join(ROOT, "tests", "golden", "config0_golden.npz"))
+
+
+def test_config0_chain_replays_reference(sp, config0):
+    """The n = 2000, m = 15 response model, 2000 samples, against the reference's own chain
+    (tests/golden/config0_golden.npz): bit-exact neighbor lists, then the FP64 chain moves at
+    exactly the reference's iterations with theta and beta equal to rounding."""
+    g = config0
+    knn = sp.mkNNIndxCB(g["coords"], 15)
+    assert np.array_equal(knn["nnIndx"], g["nnIndx"]) and np.array_equal(knn["nnIndxLU"], g["lu"])
+    assert np.array_equal(knn["nnDist"], g["nnDist"])
+    r = sp.rNNGP(g["y"], g["X"], 15, g["coords"], "exponential", g["nnIndx"], g["lu"], [2, 1], [2, 0.1], [3, 30],
+                 None, [1.0, -0.5], g["theta_start"], g["tuning"], 2000, g["normals"], g["unifs"], precision="fp64")
+    th, gth = r["p.theta.samples"], g["theta"]
+    moved = np.any(np.diff(th, axis=1) != 0, axis=0)
+    gmoved = np.any(np.diff(gth, axis=1) != 0, axis=0)
+    assert np.array_equal(moved, gmoved)
+    assert np.max(np.abs(th - gth) / np.abs(gth)) <= TOL
+    assert np.max(np.abs(r["p.beta.samples"] - g["beta"])) <= 1e-8
+
+
+def test_config0_chain_fp32r_posterior(sp, config0):
+    """The same chain in FP32R: log-target error <= 1e-6 relative, so the decisions agree with the
+    reference's except on knife-edge uniforms, and the posterior means agree within Monte Carlo
+    error (the batch-means standard error of the reference's chain, after 500 burn-in samples)."""
+    g = config0
+    r = sp.rNNGP(g["y"], g["X"], 15, g["coords"], "exponential", g["nnIndx"], g["lu"], [2, 1], [2, 0.1], [3, 30],
+                 None, [1.0, -0.5], g["theta_start"], g["tuning"], 2000, g["normals"], g["unifs"], precision="fp32r")
+    th, gth = r["p.theta.samples"], g["theta"]
+    moved = np.any(np.diff(th, axis=1) != 0, axis=0)
+    gmoved = np.any(np.diff(gth, axis=1) != 0, axis=0)
+    assert np.mean(moved == gmoved) >= 0.97
+    keep = slice(500, None)
+    for a, b in ((th, gth), (r["p.beta.samples"], g["beta"])):
+        batches = b[:, keep].reshape(b.shape[0], 15, -1).mean(axis=2)
+        se = batches.std(axis=1, ddof=1) / np.sqrt(15)
+        assert np.all(np.abs(a[:, keep].mean(axis=1) - b[:, keep].mean(axis=1)) <= 3 * se + 1e-12)
+
+
+@pytest.mark.parametrize("model,phi,alpha,nu", [(0, 6.0, 0.3, 0.0), (2, 9.0, 0.5, 1.2)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp32r", 1e-6)])
+def test_updateConjBF_matches_reference(sp, orc, model, phi, alpha, nu, precision, tol):
+    """updateConjBF (sigma^2 = 1, nugget alpha, src/cNNGP.cpp:24-69) through its own C-ABI entry
+    point, against the oracle's updateBF at theta = (1, alpha, phi[, nu]): the conjugate form is
+    the response form at unit variance."""
+    rng = np.random.default_rng(61)
+    n, m = 3000, 15
+    c = xorder(rng.uniform(size=(n, 2)))
+    o = orc.mkNNIndxCB(cm(c), m)
+    B, F = sp.updateConjBF(c, o[0], o[2], m, model, phi, alpha, nu, precision=precision)
+    Bo, Fo, _, st = orc.updateBF(cm(c), o[0], o[2], m, model, 1.0, alpha, phi, nu)
+    assert st == 0
+    assert np.max(np.abs(B - Bo)) <= tol * max(1.0, np.max(np.abs(Bo)))
+    assert np.max(np.abs(F - Fo) / Fo) <= tol

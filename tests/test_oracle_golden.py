@@ -117,3 +117,23 @@ def test_shell_sort_tie_order(orc):
     x, idx = orc.rsort_with_index([3.0, 1.0, 2.0, 1.0, 3.0, 0.5, 1.0, 2.0, 1.0, 0.5, 3.0],
                                   list(range(11)))
     assert list(x) == sorted(x)
+
+
+def test_config0_chain_replay(orc):
+    """The n = 2000, m = 15 response model with a 2000-sample chain (tests/golden/config0_golden.npz,
+    made by the reference's own C++): the oracle finds the same neighbor lists and replays the
+    chain with identical accept/reject decisions."""
+    import os
+
+    from conftest import ROOT
+
+    g = np.load(os.path.join(ROOT, "tests", "golden", "config0_golden.npz"))
+    nn, dist, lu = orc.mkNNIndxCB(cm(g["coords"]), 15, threads=os.cpu_count() or 1)
+    assert np.array_equal(nn, g["nnIndx"]) and np.array_equal(lu, g["lu"]) and np.array_equal(dist, g["nnDist"])
+    r = orc.rNNGP(g["y"], cm(g["X"]), 15, cm(g["coords"]), 0, g["nnIndx"], g["lu"], [2, 1], [2, 0.1], [3, 30],
+                  [0.5, 2.5], [1.0, -0.5], g["theta_start"], g["tuning"], 2000, g["normals"], g["unifs"],
+                  threads=os.cpu_count() or 1)
+    assert r["status"] == 0
+    assert np.array_equal(r["theta"], g["theta"])
+    assert np.max(np.abs(r["beta"] - g["beta"])) <= 1e-10
+    assert tuple(r["used"][:2]) == tuple(g["used"])
