@@ -21,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libnngp_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libspnngp_ref.so")
+RCALL_SO = os.path.join(HERE, "_build", "libspnngp_rcall.so")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -28,11 +29,14 @@ _ip = C.POINTER(C.c_int)
 COV_MODELS = ("exponential", "spherical", "matern", "gaussian")
 
 
-def build(ref: bool = False) -> None:
-    """Compile the restatement (and, with ref=True, the shim build of the reference)."""
+def build(ref: bool = False, rcall: bool = False) -> None:
+    """Compile the restatement (and, with ref=True, the shim build of the reference; with
+    rcall=True, this project's .Call layer against the same R-API stand-in)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if rcall:
+        subprocess.run(["make", "-s", "-C", HERE, "rcall"], check=True)
 
 
 def _d(a):
@@ -243,19 +247,24 @@ class Oracle(_Lib):
 
 
 class Reference(_Lib):
-    """The reference's own src/*.cpp compiled against the R-API stand-in (oracle/_ref)."""
+    """The reference's own src/*.cpp compiled against the R-API stand-in (oracle/_ref).  With
+    path=RCALL_SO the same drivers call this project's .Call layer (src/) instead: every method
+    below except spcor, updateBF, updateConjBF and Q then runs through the SEXP routines of
+    src/nngp_call.cpp."""
 
     def __init__(self, path=REF_SO):
         super().__init__(path)
         L = self.lib
         L.ref_last_error.restype = C.c_char_p
-        L.ref_spCor.restype = C.c_double
-        L.ref_spCor.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int]
-        L.ref_Q.restype = C.c_double
         L.ref_stream_set.argtypes = [_dp, C.c_long, _dp, C.c_long]
-        L.ref_updateBF.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _dp, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp]
-        L.ref_updateConjBF.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, C.c_double, C.c_double, C.c_double,
-                                       C.c_int, C.c_int, _dp, _dp]
+        if hasattr(L, "ref_spCor"):  # absent from the .Call-layer build
+            L.ref_spCor.restype = C.c_double
+            L.ref_spCor.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int]
+            L.ref_Q.restype = C.c_double
+            L.ref_updateBF.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _dp, C.c_int, C.c_double, C.c_int, _dp,
+                                       _dp, _dp]
+            L.ref_updateConjBF.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, C.c_double, C.c_double, C.c_double,
+                                           C.c_int, C.c_int, _dp, _dp]
 
     def error(self):
         return self.lib.ref_last_error().decode()

@@ -9,6 +9,13 @@
  * reference's OpenMP regions safely); every driver reports a recorded error
  * through its return value.  rnorm/runif read the host-fed streams of
  * oracle/rmath.c.
+ *
+ * Compiled with -DSHIM_CALL_ONLY (oracle/Makefile rcall) the file leaves out
+ * the four drivers that reach the reference's internal helpers (updateBF,
+ * updateConjBF, Q, spCor), so the remaining drivers -- which only call the
+ * .Call routines by name -- can be linked against any implementation of the
+ * .Call layer, such as this project's src/.  R_registerRoutines keeps the
+ * registered table for inspection.
  */
 #include <cstdarg>
 #include <cstdio>
@@ -25,6 +32,7 @@
 #include "R.h"
 #include "Rinternals.h"
 #include "Rmath.h"
+#include "R_ext/Rdynload.h"
 
 extern "C" {
 double or_bessel_k(double x, double nu);
@@ -131,6 +139,24 @@ double bessel_k_ex(double x, double alpha, double expo, double *bk) {
 }
 void rsort_with_index(double *x, int *indx, int n) { or_rsort_with_index(x, indx, n); }
 
+/* routine registration */
+static const R_CallMethodDef *g_routines = nullptr;
+int R_registerRoutines(DllInfo *info, const void *croutines, const R_CallMethodDef *callRoutines,
+                       const void *fortranRoutines, const void *externalRoutines) {
+  (void)info;
+  (void)croutines;
+  (void)fortranRoutines;
+  (void)externalRoutines;
+  g_routines = callRoutines;
+  return 1;
+}
+int R_useDynamicSymbols(DllInfo *info, Rboolean value) {
+  (void)info;
+  (void)value;
+  return 1;
+}
+const R_CallMethodDef *shim_call_routines(void) { return g_routines; }
+
 } /* extern "C" */
 
 /* ------------------------------------------------------------ reference entry points */
@@ -147,6 +173,7 @@ SEXP rNNGPPredict(SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SE
 SEXP rNNGPReplicated(SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP, SEXP,
                      SEXP, SEXP);
 }
+#ifndef SHIM_CALL_ONLY
 /* C++-linkage helpers of the reference (src/rNNGP.cpp:46, src/cNNGP.cpp:24, src/util.cpp:208,261) */
 double updateBF(double *B, double *F, double *c, double *C, double *coords, int *nnIndx,
                 int *nnIndxLU, int n, int m, double *theta, int tauSqIndx, int sigmaSqIndx,
@@ -156,6 +183,7 @@ void updateConjBF(double *B, double *F, double *c, double *C, double *coords, in
                   double *bk, double nuMax);
 double spCor(double &D, double &phi, double &nu, int &covModel, double *bk);
 double Q(double *B, double *F, double *u, double *v, int n, int *nnIndx, int *nnIndxLU);
+#endif
 
 /* wrap caller memory (no copy) */
 static SEXP wrap_real(const double *p, long n) {
@@ -206,6 +234,10 @@ static void copy_out(SEXP v, double *dst) {
 extern "C" {
 
 const char *ref_last_error(void) { return g_error.c_str(); }
+void ref_clear_error(void) {
+  std::lock_guard<std::mutex> lk(g_alloc_mu);
+  g_error.clear();
+}
 void ref_set_verbose(int v) { g_verbose = v; }
 void ref_stream_set(const double *normals, long n_norm, const double *unifs, long n_unif) {
   or_stream_set(normals, n_norm, unifs, n_unif);
@@ -240,6 +272,7 @@ int ref_mkUIndx(int n, int m, const int *nnIndx, int *uIndx, int *uIndxLU, int *
   return end_call();
 }
 
+#ifndef SHIM_CALL_ONLY
 double ref_spCor(double D, double phi, double nu, int covModel) {
   double bk[64];
   return spCor(D, phi, nu, covModel, bk);
@@ -288,6 +321,8 @@ double ref_Q(const double *B, const double *F, const double *u, const double *v,
 }
 
 /* src/rNNGP.cpp:105-109 argument order; outputs p x nSamples, nTheta x nSamples, n x nRep */
+#endif
+
 int ref_rNNGP(const double *y, const double *X, int p, int n, int m, const double *coords,
               int covModel, const int *nnIndx, const int *nnIndxLU, const double *sigmaSqIG,
               const double *tauSqIG, const double *phiUnif, const double *nuUnif,
