@@ -420,17 +420,20 @@ def section_accuracy(sp, ctx, dev, n=N, ms=(15, 32), seed=2024, reps=3):
                 ctx.call("nngp_kernel_time", C.byref(kms), None)
                 ctx.call("nngp_set_kernel_timing", 0)
                 resolved = ctx.fp32r_resolved()[0] if pc else 0
+                tiers = ctx.fp32r_tiers() if pc else (0, 0)
                 ll = ll_of(d_ld.item(), d_G.cpu().numpy().reshape(nv, nv))
                 B, F, _ = sp.updateBF(c, nn, lu, m, model, theta, prec, ctx=ctx)
-                res[prec] = (ll, B, F, ev0.elapsed_time(ev1) / reps, kms.value / reps, resolved)
-            ll64, B64, F64, p64, _, _ = res["fp64"]
-            ll32, B32, F32, p32, k32, nres = res["fp32r"]
+                res[prec] = (ll, B, F, ev0.elapsed_time(ev1) / reps, kms.value / reps, resolved, tiers)
+            ll64, B64, F64, p64, _, _, _ = res["fp64"]
+            ll32, B32, F32, p32, k32, nres, ntiers = res["fp32r"]
             rows.append({"m": m, "model": model, "range": rng_eff, "theta": list(theta),
                          "loglik_rel_err": abs(ll32 - ll64) / abs(ll64),
                          "F_max_rel_err": float(np.max(np.abs(F32 - F64) / F64)),
                          "B_max_err_rel_max_abs": float(np.max(np.abs(B32 - B64)) / max(1.0, np.max(np.abs(B64)))),
                          "pass_ms_fp64": p64, "pass_ms_fp32r": p32, "fp32r_speedup": p64 / p32,
-                         "fp32r_primary_kernel_ms": k32, "fp32r_resolved_in_fp64": nres, "knn_seconds": knn_s})
+                         "fp32r_primary_kernel_ms": k32, "fp32r_resolved": nres,
+                         "fp32r_resolved_double_float": ntiers[0], "fp32r_resolved_fp64": ntiers[1],
+                         "knn_seconds": knn_s})
             del B64, F64, B32, F32
         del d_nn, d_lu
     worst = max(r["loglik_rel_err"] for r in rows)
@@ -442,7 +445,9 @@ def section_accuracy(sp, ctx, dev, n=N, ms=(15, 32), seed=2024, reps=3):
             "within_1e-6": bool(worst <= 1e-6 and worst_f <= 1e-6),
             "note": "pass_ms: the whole fused likelihood pass timed with CUDA events on the launching stream "
                     f"(mean of {reps}); fp32r_primary_kernel_ms: its FP32R kernel alone; the gaussian cases "
-                    "(1e-6 nugget) are too ill-conditioned for a float factor and run almost entirely in FP64"}
+                    "(1e-6 nugget) are too ill-conditioned for a float factor: their flagged locations are "
+                    "re-solved in double-float on the FP32 pipe for m <= 16 and in FP64 for m > 16 "
+                    "(fp32r_resolved_double_float / fp32r_resolved_fp64)"}
 
 
 def section_config0(sp, ctx, skip_cpu=False):

@@ -261,11 +261,19 @@ int nngp_kernel_time(nngp_ctx *ctx, double *ms, int64_t *launches);
 
 /* Precision diagnostic, no counterpart in the reference: the number of
  * locations that the last FP32R pass of the single-dataset entry points
- * (updateBF, loglik_gram and their _dev forms) handed to the FP64 kernel --
- * float pivot failed, error estimate above the bound, or F below 1e-6 of
+ * (updateBF, loglik_gram and their _dev forms) re-solved in higher precision
+ * -- float pivot failed, error estimate above the bound, or F below 1e-6 of
  * sigma^2 + tau^2 -- and the number of locations that pass covered; 0 and 0
  * after an FP64 pass.  Synchronises the context's stream. */
 int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations);
+
+/* Precision diagnostic, no counterpart in the reference: how the locations
+ * counted by nngp_fp32r_resolved were re-solved -- in double-float arithmetic
+ * on the FP32 pipe (neighbor bounds m <= 16: the flagged locations of the
+ * register kernel go there first) or in FP64 (every flagged location for
+ * 16 < m <= 32; for m <= 16 the 64-location tiles holding a location the
+ * double-float solve could not certify).  Synchronises the context's stream. */
+int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);
 
 /* Launch-shape autotuner of the FP32R B/F kernel for m <= 16, no counterpart
  * in the reference (it stands in for the reference's n.omp.threads tuning).

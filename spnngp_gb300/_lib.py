@@ -63,6 +63,7 @@ _SIGNATURES = {
     "nngp_set_kernel_timing": (_i, [_vp, _i]),
     "nngp_kernel_time": (_i, [_vp, _dp, C.POINTER(_i64)]),
     "nngp_fp32r_resolved": (_i, [_vp, C.POINTER(_i64), C.POINTER(_i64)]),
+    "nngp_fp32r_tiers": (_i, [_vp, C.POINTER(_i64), C.POINTER(_i64)]),
     "nngp_set_autotune": (_i, [_vp, _i]),
     "nngp_set_launch_shape": (_i, [_vp, _i, _i, _i]),
     "nngp_autotune_report": (_i, [_vp, C.c_char_p, _i]),
@@ -204,6 +205,12 @@ class Context:
         """Forces the FP32R register kernel's launch shape (warps_per_block 0: autotune again);
         tmem selects the variant keeping the covariance's low-order parts in tensor memory."""
         self.call("nngp_set_launch_shape", int(warps_per_block), int(grid_mode), 1 if tmem else 0)
+
+    def fp32r_tiers(self) -> tuple[int, int]:
+        """(re-solved in double-float, re-solved in FP64) of the last single-dataset FP32R pass."""
+        a, b = _i64(), _i64()
+        self.call("nngp_fp32r_tiers", C.byref(a), C.byref(b))
+        return int(a.value), int(b.value)
 
     def fp32r_resolved(self) -> tuple[int, int]:
         """(locations re-solved in FP64, locations covered) of the last single-dataset FP32R pass."""

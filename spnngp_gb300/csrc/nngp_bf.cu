@@ -35,6 +35,10 @@ namespace nngp_bfwd {
 template <int M, int MODE, int COV>
 int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
 }  // namespace nngp_bfwd
+namespace nngp_bfdf {
+template <int MODE, int COV>
+int launch_df(nngp_ctx *ctx, const BFPlan *pl);
+}  // namespace nngp_bfdf
 using namespace nngp_bf;
 
 namespace {
@@ -321,6 +325,20 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm, t1 - t0, tm), false, t0, t1, tm);
 }
 
+// The double-float re-solve of a register-kernel plan's flagged tiles (nngp_bfdf_kernel.cuh).
+int launch_df_any(nngp_ctx *ctx, const BFPlan *pl) {
+  using nngp_bfdf::launch_df;
+  const bool fused = pl->mode == 1;
+  switch (pl->cov) {
+    case NNGP_COV_EXP: return fused ? launch_df<1, NNGP_COV_EXP>(ctx, pl) : launch_df<0, NNGP_COV_EXP>(ctx, pl);
+    case NNGP_COV_SPH: return fused ? launch_df<1, NNGP_COV_SPH>(ctx, pl) : launch_df<0, NNGP_COV_SPH>(ctx, pl);
+    case NNGP_COV_MAT_HALF:
+      return fused ? launch_df<1, NNGP_COV_MAT_HALF>(ctx, pl) : launch_df<0, NNGP_COV_MAT_HALF>(ctx, pl);
+    case NNGP_COV_GAU: return fused ? launch_df<1, NNGP_COV_GAU>(ctx, pl) : launch_df<0, NNGP_COV_GAU>(ctx, pl);
+    default: return fused ? launch_df<1, NNGP_COV_ANY>(ctx, pl) : launch_df<0, NNGP_COV_ANY>(ctx, pl);
+  }
+}
+
 // Primary pass over tiles [t0, t1), or (fallback_pass) the FP64 re-solve of the recorded tiles.
 int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
   if (fp32r && !fallback_pass) return pl->reg_m > 0 ? run_reg(ctx, pl, t0, t1) : warp_call(ctx, pl, t0, t1);
@@ -398,6 +416,15 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
     pl->d_fb_words = (unsigned *)own(sizeof(unsigned) * (1 + (size_t)pl->tiles_fb));
     pl->d_fb_list = (int *)own(sizeof(int) * (size_t)(pl->tiles_fb > 0 ? pl->tiles_fb : 1));
     if (!pl->d_fb_words || !pl->d_fb_list) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+    if (pl->reg_m > 0) {  // flagged tiles: double-float kernel first, then FP64 for what it cannot certify
+      pl->d_fb64_list = (int *)own(sizeof(int) * (size_t)(pl->tiles_fb > 0 ? pl->tiles_fb : 1));
+      pl->d_fb64_locs = (unsigned long long *)own(2 * sizeof(unsigned long long));
+      if (!pl->d_fb64_list || !pl->d_fb64_locs) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+      pl->d_fb64_count = reinterpret_cast<int *>(pl->d_fb64_locs + 1);
+    } else {
+      pl->d_fb64_list = pl->d_fb_list;
+      pl->d_fb64_count = (int *)pl->d_fb_words;
+    }
     size_t fb = 0;
     for (const PassEval &e : evals) fb += (size_t)datas[e.data].n;
     pl->flags_bytes = fb;
@@ -461,6 +488,8 @@ int nngp_bf_begin(nngp_ctx *ctx, const BFPlan *pl) {
   if (pl->precision == NNGP_FP32R) {
     NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_flags, 0, pl->flags_bytes, ctx->stream));
     NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_fb_words, 0, sizeof(unsigned) * (1 + (size_t)pl->tiles_fb), ctx->stream));
+    if (pl->d_fb64_locs)
+      NNGP_CUDA_TRY(ctx, cudaMemsetAsync(pl->d_fb64_locs, 0, 2 * sizeof(unsigned long long), ctx->stream));
   }
   return NNGP_OK;
 }
@@ -492,7 +521,9 @@ int nngp_bf_primary(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
 int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   int st;
   const bool fp32r = pl->precision == NNGP_FP32R;
-  // FP32R: the FP64 re-solve of the recorded tiles, folded into the same fixed-order sums
+  // FP32R: the re-solve of the recorded tiles (register-kernel plans: double-float first, FP64
+  // for the tiles it cannot certify), folded into the same fixed-order sums
+  if (fp32r && pl->reg_m > 0 && (st = launch_df_any(ctx, pl))) return st;
   if (fp32r && (st = launch_pass(ctx, pl, false, true, 0, 0))) return st;
   reduce_chunks_kernel<<<pl->njobs * pl->red_chunks, 256, 0, ctx->stream>>>(
       pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr, fp32r ? pl->d_fb_words + 1 : nullptr,
@@ -560,6 +591,23 @@ int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len) {
     buf[k] = 0;
   }
   return (int)ctx->tuned.size();
+}
+int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64) {
+  if (!ctx || !double_float || !fp64) return NNGP_ERR_ARG;
+  int64_t total = 0, locations = 0;
+  const int st = nngp_fp32r_resolved(ctx, &total, &locations);
+  if (st) return st;
+  *double_float = 0;
+  *fp64 = total;
+  const BFPlan *pl = ctx->cache_plan;
+  if (pl && pl->precision == NNGP_FP32R && pl->d_fb64_locs) {
+    unsigned long long h = 0;
+    NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&h, pl->d_fb64_locs, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    *fp64 = (int64_t)h;
+    *double_float = total - (int64_t)h;
+  }
+  return NNGP_OK;
 }
 int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations) {
   if (!ctx || !resolved || !locations) return NNGP_ERR_ARG;

@@ -290,8 +290,8 @@ int launch_one(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int 
   kern<<<grid, TPB, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, jobs, pl->njobs,
                                          fallback_pass ? 0 : t0, fallback_pass ? pl->tiles_fb : t1, pl->nv,
                                          pl->d_status, fallback_pass ? 1 : 0,
-                                         fallback_pass ? pl->d_fb_list : nullptr,
-                                         fallback_pass ? (const int *)pl->d_fb_words : nullptr);
+                                         fallback_pass ? pl->d_fb64_list : nullptr,
+                                         fallback_pass ? (const int *)pl->d_fb64_count : nullptr);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }

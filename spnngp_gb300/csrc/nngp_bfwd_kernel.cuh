@@ -224,7 +224,7 @@ int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, i
   bfwd_kernel<M, MODE, COV><<<grid, 32 * kWarpsPerBlock, smem, ctx->stream>>>(
       pl->d_datas, pl->d_thetas, fallback_pass ? pl->d_jobs_fb : pl->d_jobs, pl->njobs, fallback_pass ? 0 : t0,
       fallback_pass ? pl->tiles_fb : t1, pl->nv, pl->d_status, fallback_pass ? 1 : 0,
-      fallback_pass ? pl->d_fb_list : nullptr, fallback_pass ? (const int *)pl->d_fb_words : nullptr);
+      fallback_pass ? pl->d_fb64_list : nullptr, fallback_pass ? (const int *)pl->d_fb64_count : nullptr);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
 }

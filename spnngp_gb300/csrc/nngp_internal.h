@@ -238,6 +238,12 @@ struct BFPlan {
   // FP32R: [count | marks (tiles_fb)] words and the list of FP64 tiles to re-solve
   unsigned *d_fb_words = nullptr;
   int *d_fb_list = nullptr;
+  // the tiles the FP64 kernel re-solves: the list above, or (register-kernel plans, whose
+  // flagged tiles go to the double-float kernel first) the tiles that kernel could not certify,
+  // with the number of flagged locations in them
+  int *d_fb64_list = nullptr;
+  int *d_fb64_count = nullptr;
+  unsigned long long *d_fb64_locs = nullptr;
   // fixed-order reduction: the tiles of a job are summed in chunks of 1024 tiles (one block
   // each; red_chunks is the most any job has), then the chunk sums in order
   int red_chunks = 0;

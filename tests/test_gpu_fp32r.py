@@ -220,3 +220,32 @@ def test_resolved_count_reports_fp64_handoffs(sp, orc, m):
     assert n_hard == 4000 and r_hard >= 2000
     sp.updateBF(c, o[0], o[2], m, "gaussian", (1.0, 1e-6, 3.462), "fp64")
     assert ctx.fp32r_resolved() == (0, 0)
+
+
+@pytest.mark.parametrize("m", [10, 15, 16])
+@pytest.mark.parametrize("phi", [34.62, 3.462])
+def test_double_float_tier_on_ill_conditioned_gaussian(sp, orc, m, phi):
+    """Gaussian covariance with a 1e-6 nugget (condition numbers ~1e7): nearly every location is
+    flagged by the float solve; the double-float re-solve takes them (FP64 only for tiles it
+    cannot certify), and F stays within 1e-6 of its exact value (extended precision) and the
+    log-likelihood within 1e-6 of the FP64 form."""
+    from test_gpu_parity_scale import _exact_F
+
+    c, X, y = dataset(4000, 300 + m)
+    o = orc.mkNNIndxCB(cm(c), m)
+    theta = (1.0, 1e-6, phi)
+    ctx = sp.default_context()
+    _, F32, _ = sp.updateBF(c, o[0], o[2], m, "gaussian", theta, "fp32r")
+    n_df, n_64 = ctx.fp32r_tiers()
+    resolved, _ = ctx.fp32r_resolved()
+    assert n_df + n_64 == resolved and resolved > 0.5 * len(c)
+    assert n_df > 0.5 * resolved  # the double-float tier takes most of them
+    Ft = _exact_F(c, o[0], o[2], m, theta)
+    assert float(np.max(np.abs(F32 - Ft) / Ft)) <= 1e-6
+    V = np.column_stack([X, y])
+    beta = np.array([1.0, -0.5])
+    ll = {}
+    for prec in ("fp64", "fp32r"):
+        ld, G = sp.loglik_gram(c, o[0], o[2], m, V, "gaussian", theta, prec)
+        ll[prec] = -0.5 * (ld + beta @ G[:2, :2] @ beta - 2 * beta @ G[:2, 2] + G[2, 2])
+    assert abs(ll["fp32r"] - ll["fp64"]) <= 1e-6 * abs(ll["fp64"])
