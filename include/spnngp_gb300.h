@@ -232,6 +232,19 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m,
                          const int *nnIndxLU, const double *beta, const double *theta,
                          int nSamples, const double *normals, int precision, double *yRep);
 
+/* Exact posterior draws of the conjugate model at its selected parameter set
+ * (R/spConjNNGP.R:423-436, with rigamma and rmvn of R/util.R:1-11): for every
+ * sample s, sigma^2 = b / gammas[s], beta = bBInv bb + sigma L z_s (L the lower
+ * Cholesky factor of bBInv, z_s = normals[s p .. s p + p)), tau^2 = alpha
+ * sigma^2.  gammas are host-fed Gamma(a, 1) variates (the draw behind R's
+ * rgamma(1, shape = a, rate = b) = gammas[s] / b), bb and bBInv (p x p, lower
+ * triangle read) as nngp_cNNGP returns them, a and b its ab.  Output samples
+ * nSamples x (p + 2) column-major: beta, sigma.sq, tau.sq per row, the
+ * layout of R's p.beta.theta.samples. */
+int nngp_conj_posterior_samples(nngp_ctx *ctx, int p, const double *bb, const double *bBInv, double a, double b,
+                                double alpha, int nSamples, const double *gammas, const double *normals,
+                                double *samples);
+
 /* ----------------------------------------------- device-resident variants
  * Same contracts as above; every pointer is device memory and the call is
  * asynchronous on the context stream (status and logDet/gram are available

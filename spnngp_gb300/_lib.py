@@ -52,6 +52,7 @@ _SIGNATURES = {
     "nngp_rNNGPPredict": (_i, [_vp, _dp, _dp, _dp, _i, _i, _i, _dp, _dp, _i, _ip, _dp, _dp, _i, _i, _dp, _i,
                                _dp]),
     "nngp_rNNGPReplicated": (_i, [_vp, _dp, _i, _i, _i, _dp, _i, _ip, _ip, _dp, _dp, _i, _dp, _i, _dp]),
+    "nngp_conj_posterior_samples": (_i, [_vp, _i, _dp, _dp, _d, _d, _d, _i, _dp, _dp, _dp]),
     # device-resident variants: every array argument is a device pointer (theta stays on the host)
     "nngp_updateBF_dev": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp, _vp]),
     "nngp_loglik_gram_dev": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _i, _dp, _i, _vp, _vp]),

@@ -416,15 +416,12 @@ def spConjNNGP(y, X, coords, knots=None, n_neighbors=15, theta_alpha=None, sigma
                                 "nn.indx": nn_indx, "nn.indx.lu": nn_indx_lu, "ord": ord_,
                                 "nn.indx.run.time": nn_run_time}
     # exact posterior sampling (R/spConjNNGP.R:423-436): sigma^2 ~ IG(a, b), beta | sigma^2 ~
-    # N(bB.inv bb, sigma^2 bB.inv), tau^2 = alpha sigma^2; batched (all inverse-gamma draws,
-    # then all normals: O(n.samples p^2) work, no per-sample loop)
+    # N(bB.inv bb, sigma^2 bB.inv), tau^2 = alpha sigma^2, on the device from host-fed Gamma(a, 1)
+    # variates and normals (one gamma and p normals per sample)
     if n_samples > 0:
-        Lb = np.linalg.cholesky(Binv)
-        bhat = Binv @ res["bb"]
         alpha = ta[0, 1]
-        s2 = b / gen.gamma(a, size=n_samples)
-        beta = bhat + np.sqrt(s2)[:, None] * (gen.standard_normal((n_samples, p)) @ Lb.T)
-        draws = np.column_stack([beta, s2, alpha * s2])
+        draws = core.conj_posterior_samples(res["bb"], Binv, a, b, alpha, gen.gamma(a, size=n_samples),
+                                            gen.standard_normal(n_samples * p), ctx=ctx)
         res["p.beta.theta.samples"] = draws
         if fit_rep:
             inv_o = np.argsort(ord_, kind="stable")

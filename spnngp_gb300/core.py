@@ -302,6 +302,22 @@ def rNNGPReplicated(X, m: int, coords, cov_model, nn_indx, nn_indx_lu, beta, the
     return {"y.rep.samples": yr.reshape(nS, n).T}
 
 
+def conj_posterior_samples(bb, bB_inv, a: float, b: float, alpha: float, gammas, normals,
+                           ctx: Context | None = None) -> np.ndarray:
+    """Exact posterior draws of the conjugate model (R/spConjNNGP.R:423-436) on the device: rows
+    (beta, sigma.sq, tau.sq), one per Gamma(a, 1) variate in gammas; normals holds p standard
+    normals per sample.  bB_inv is p x p (its lower triangle is read)."""
+    bb = f64(bb)
+    p = len(bb)
+    g = f64(gammas)
+    ns = len(g)
+    Bl = f64(np.asarray(bB_inv, np.float64).T.reshape(-1))  # column-major
+    out = np.zeros(max(ns * (p + 2), 1))
+    _ctx(ctx).call("nngp_conj_posterior_samples", p, dptr(bb), dptr(Bl), float(a), float(b), float(alpha), ns,
+                   dptr(g), dptr(f64(normals)), dptr(out))
+    return out[: ns * (p + 2)].reshape(p + 2, ns).T
+
+
 def cNNGP_multi(problems, m: int, sigma_sq_IG, cov_model, precision="fp64", want_pred=True,
                 ctx: Context | None = None) -> list:
     """Batched conjugate fits (nngp_cNNGP_multi): every (problem, parameter set) in one fused

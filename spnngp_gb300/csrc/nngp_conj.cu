@@ -356,6 +356,69 @@ int nngp_rNNGPPredict(nngp_ctx *ctx, const double *X, const double *y, const dou
   return NNGP_OK;
 }
 
+namespace {
+// Exact posterior draws of the conjugate model at one parameter set (R/spConjNNGP.R:423-436 and
+// R/util.R:1-11): sigma^2 = b / g with g ~ Gamma(a, 1) host-fed (rigamma's 1 / rgamma(a, rate b)),
+// beta = B^-1 bb + sigma L z with L the lower Cholesky factor of B^-1 (rmvn's z'chol(V),
+// V = sigma^2 B^-1), tau^2 = alpha sigma^2.  Every block recomputes the p x p factor and mean in
+// shared memory (p <= 8); then one thread per sample.  out is nSamples x (p + 2), column-major
+// (the rows of R's p.beta.theta.samples: beta, sigma.sq, tau.sq).
+__global__ void conj_posterior_kernel(int p, const double *__restrict__ bb, const double *__restrict__ Binv, double b,
+                                      double alpha, int nSamples, const double *__restrict__ gam,
+                                      const double *__restrict__ z, double *__restrict__ out, int *__restrict__ bad) {
+  __shared__ double L[NNGP_MAX_NV * NNGP_MAX_NV], mu[NNGP_MAX_NV];
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < p; j++)
+      for (int i = 0; i < p; i++) L[j * p + i] = (i >= j) ? Binv[j * p + i] : 0.0;
+    small_symv(L, p, bb, mu);  // B^-1 bb from the lower triangle
+    if (!small_potrf(L, p)) *bad = 1;
+    for (int j = 0; j < p; j++)
+      for (int i = 0; i < j; i++) L[j * p + i] = 0.0;  // the strict upper part is not the factor's
+  }
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nSamples) return;
+  const double s2 = b / gam[s];
+  const double sd = sqrt(s2);
+  const double *zs = z + (size_t)s * p;
+  for (int j = 0; j < p; j++) {
+    double acc = 0.0;
+    for (int i = 0; i <= j; i++) acc += L[i * p + j] * zs[i];
+    out[(size_t)j * nSamples + s] = mu[j] + sd * acc;
+  }
+  out[(size_t)p * nSamples + s] = s2;
+  out[(size_t)(p + 1) * nSamples + s] = alpha * s2;
+}
+}  // namespace
+
+int nngp_conj_posterior_samples(nngp_ctx *ctx, int p, const double *bb, const double *bBInv, double a, double b,
+                                double alpha, int nSamples, const double *gammas, const double *normals,
+                                double *samples) {
+  if (!ctx) return NNGP_ERR_ARG;
+  if (p < 1 || p > NNGP_MAX_NV) return nngp_fail(ctx, NNGP_ERR_ARG, "1 <= p <= 8 required");
+  if (nSamples <= 0) return NNGP_OK;
+  if (!(a > 0.0) || !(b > 0.0)) return nngp_fail(ctx, NNGP_ERR_ARG, "the inverse-gamma parameters must be positive");
+  cudaSetDevice(ctx->device);
+  Tmp T(ctx);
+  const double *dbb = (const double *)T.up(bb, sizeof(double) * p);
+  const double *dB = (const double *)T.up(bBInv, sizeof(double) * p * p);
+  const double *dg = (const double *)T.up(gammas, sizeof(double) * (size_t)nSamples);
+  const double *dz = (const double *)T.up(normals, sizeof(double) * (size_t)nSamples * p);
+  double *dout = (double *)T.up(nullptr, sizeof(double) * (size_t)nSamples * (p + 2));
+  int *dbad = (int *)T.up(nullptr, sizeof(int));
+  if (T.bad) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+  NNGP_CUDA_TRY(ctx, cudaMemsetAsync(dbad, 0, sizeof(int), ctx->stream));
+  conj_posterior_kernel<<<nb(nSamples, 128), 128, 0, ctx->stream>>>(p, dbb, dB, b, alpha, nSamples, dg, dz, dout, dbad);
+  NNGP_LAUNCH_CHECK(ctx);
+  int hbad = 0;
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(&hbad, dbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaMemcpyAsync(samples, dout, sizeof(double) * (size_t)nSamples * (p + 2),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+  NNGP_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (hbad) return nngp_fail(ctx, NNGP_ERR_NOT_SPD, "conjugate posterior: bB.inv is not positive definite");
+  return NNGP_OK;
+}
+
 int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, const double *coords,
                          int covModel, const int *nnIndx, const int *nnIndxLU, const double *beta,
                          const double *theta, int nSamples, const double *normals, int precision,

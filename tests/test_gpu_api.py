@@ -139,3 +139,33 @@ def test_spConjNNGP_posterior_samples_and_replicates():
     sd = np.sqrt(np.diag(fit["beta.var"]))
     assert np.all(np.abs(d[:, :p].mean(axis=0) - fit["beta.hat"]) <= 5 * sd / np.sqrt(ns))
     assert fit["y.hat.samples"].shape == (800, ns) and fit["y.rep.samples"].shape == (800, ns)
+
+
+def test_conjugate_posterior_samples_on_device(sp):
+    """The exact posterior draws of the conjugate model (R/spConjNNGP.R:423-436) made on the device
+    from host-fed Gamma(a, 1) variates and normals: each row equals the formula
+    sigma^2 = b / g, beta = bB.inv bb + sigma chol(bB.inv) z, tau^2 = alpha sigma^2."""
+    rng = np.random.default_rng(81)
+    p, ns = 3, 5000
+    A = rng.normal(size=(p, p))
+    Binv = A @ A.T + p * np.eye(p)
+    bb = rng.normal(size=p)
+    a, b, alpha = 12.5, 3.25, 0.4
+    g = rng.gamma(a, size=ns)
+    z = rng.standard_normal(ns * p)
+    got = sp.core.conj_posterior_samples(bb, Binv, a, b, alpha, g, z)
+    L = np.linalg.cholesky(Binv)
+    s2 = b / g
+    beta = Binv @ bb + np.sqrt(s2)[:, None] * (z.reshape(ns, p) @ L.T)
+    want = np.column_stack([beta, s2, alpha * s2])
+    assert got.shape == (ns, p + 2)
+    assert np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want))) <= 1e-12
+    # the draws' moments match the posterior: E[sigma^2] = b / (a - 1), Var(beta | .) = E[sigma^2] bB.inv
+    assert abs(got[:, p].mean() - b / (a - 1)) <= 5 * np.std(got[:, p]) / np.sqrt(ns)
+    assert np.allclose(np.cov(got[:, :p].T), b / (a - 1) * Binv, rtol=0.15, atol=0.05)
+
+
+def test_conjugate_posterior_rejects_non_spd(sp):
+    with pytest.raises(sp.NNGPError) as e:
+        sp.core.conj_posterior_samples(np.ones(2), -np.eye(2), 3.0, 1.0, 0.5, np.ones(4), np.zeros(8))
+    assert e.value.status == 3
