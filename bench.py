@@ -280,14 +280,25 @@ def section_mcmc_batch(sp, ctx, dev, iters, n_inst=256, seed=77):
             P.nSamples = n_iter
         ctx.call("nngp_rNNGP_batch", n_inst, C.cast(probs, C.c_void_p), 2, 1, resident)
 
-    run(1, 3)  # warm-up: plans, graph capture, allocator pool
+    run(1, 3)  # warm-up: kernels loaded, tuning, allocator pool
     torch.cuda.synchronize()
+    # a short call: its time is the one-off cost of a call (plans, graph capture, first passes)
+    # plus its few iterations, which the long call's per-iteration time separates out
+    short = 10
+    t0 = time.perf_counter()
+    run(1, short)
+    dt_short = time.perf_counter() - t0
+    e2e_iters = min(iters, 200)
+    run(1, e2e_iters)
+    acc_e2e = [P.nAccept for P in probs]
     ctx.reset_launches()
     t0 = time.perf_counter()
     run(1, iters)
     dt = time.perf_counter() - t0
     launches = ctx.launches
     acc = [P.nAccept for P in probs]
+    per_iter = (dt - dt_short) / max(iters - short, 1)
+    setup = max(dt_short - short * per_iter, 0.0)
     # the same chains through the host-memory form of the call (uploads and sample readback inside)
     hprobs = (MCMCProblem * n_inst)()
     hkeep = []
@@ -297,10 +308,11 @@ def section_mcmc_batch(sp, ctx, dev, iters, n_inst=256, seed=77):
         H = hprobs[k]
         C.memmove(C.addressof(H), C.addressof(src), C.sizeof(MCMCProblem))
         nT = 4 if src.covModel == 2 else 3
+        H.nSamples = e2e_iters
         ha = {"y": y, "X": np.ascontiguousarray(X.T).reshape(-1), "coords": np.ascontiguousarray(c.T).reshape(-1),
               "nnIndx": nn, "nnIndxLU": lu, "normals": dev_arrays["normals"].cpu().numpy(),
-              "unifs": dev_arrays["unifs"].cpu().numpy(), "betaSamples": np.zeros(2 * iters),
-              "thetaSamples": np.zeros(nT * iters)}
+              "unifs": dev_arrays["unifs"].cpu().numpy(), "betaSamples": np.zeros(2 * e2e_iters),
+              "thetaSamples": np.zeros(nT * e2e_iters)}
         for name, a in ha.items():
             setattr(H, name, a.ctypes.data)
         hkeep.append(ha)
@@ -309,20 +321,23 @@ def section_mcmc_batch(sp, ctx, dev, iters, n_inst=256, seed=77):
     t0 = time.perf_counter()
     ctx.call("nngp_rNNGP_batch", n_inst, C.cast(hprobs, C.c_void_p), 2, 1, 0)
     e2e_dt = time.perf_counter() - t0
-    same = all(hprobs[k].nAccept == acc[k] for k in range(n_inst))
+    same = all(hprobs[k].nAccept == acc_e2e[k] for k in range(n_inst))
     return {
         "workload": f"{n_inst} independent response-model chains, n log-uniform [500, 50000] (total {total_n}), "
                     "m cycling 10/15/20, cov.model cycling exponential/spherical/gaussian/matern(nu 0.5/1.5/2.5 "
                     "fixed), y = X beta + w + eps with w an NNGP draw, FP32R",
         "iterations": iters, "seconds": dt, "iterations_per_s": iters / dt, "ms_per_iteration": dt * 1e3 / iters,
-        "solves_per_s": total_n * iters / dt, "gpu_launches": int(launches),
-        "launches_per_iteration": launches / iters,
+        "solves_per_s": total_n * iters / dt,
+        "replay_ms_per_iteration": per_iter * 1e3, "replay_solves_per_s": total_n / per_iter,
+        "call_setup_s": setup,
+        "gpu_launches": int(launches), "launches_per_iteration": launches / iters,
         "mean_accept_rate": float(np.mean(acc)) / iters,
-        "e2e": {"seconds": e2e_dt, "iterations_per_s": iters / e2e_dt, "h2d_bytes": int(h2d), "d2h_bytes": int(d2h),
-                "same_accept_counts_as_resident": same},
+        "e2e": {"iterations": e2e_iters, "seconds": e2e_dt, "iterations_per_s": e2e_iters / e2e_dt,
+                "h2d_bytes": int(h2d), "d2h_bytes": int(d2h), "same_accept_counts_as_resident": same},
         "data_generation_s": gen_s,
-        "iterations_note": "the timed call includes plan building and graph capture; 5000 iterations scale "
-                           "linearly from this",
+        "note": "seconds: one call running every chain for all iterations (plans, graph capture and the "
+                "per-iteration graph replays); replay_ms_per_iteration and call_setup_s split it using a "
+                f"{short}-iteration call",
     }
 
 
@@ -611,39 +626,52 @@ def section_conj_sweep(sp, ctx, orc=None, n=200_000, seed=91):
     return out
 
 
-def section_serving(sp, ctx, rates=(10, 50, 100, 200, 500), seed=55, max_requests=200, pool=32):
+def section_serving(sp, ctx, warm_rates=(10, 50, 100, 200, 500, 1000, 2000), cold_rates=(10, 50, 200), seed=55,
+                    max_requests=200, pool=32):
     """Serving: Poisson streams of spConjNNGP fit + predict requests, n log-uniform in [1e3, 5e5],
     prediction sets of U[1e3, 1e5] uniform points, m = 15, exponential, (phi, alpha) from the
     50 x 20 grid, HBM budget 150 GB; the continuous-batching server against the plain
-    per-request form on the same arrival times."""
+    per-request form on the same arrival times.  Warm streams draw their datasets from a pool
+    of 32 that the server keeps resident (the neighbor.info reuse); in cold streams every
+    request brings a dataset of its own, so its upload, ordering and neighbor search are inside
+    its latency."""
     from spnngp_gb300 import serving as S
 
     rng = np.random.default_rng(seed)
-    datasets = []
-    for k in range(pool):
+    phis, alphas = np.linspace(3, 30, 50), np.linspace(0.05, 2, 20)
+
+    def make_dataset():
         n = int(np.exp(rng.uniform(np.log(1e3), np.log(5e5))))
         c = rng.uniform(size=(n, 2))
         X = np.column_stack([np.ones(n), rng.normal(size=n)])
         y = X @ np.array([1.0, -0.5]) + np.sin(5 * c[:, 0]) * np.cos(3 * c[:, 1]) + rng.normal(scale=0.3, size=n)
-        datasets.append((c, X, y))
-    preds = []
-    for k in range(pool):
-        n0 = int(rng.uniform(1e3, 1e5))
-        preds.append((rng.uniform(size=(n0, 2)), np.column_stack([np.ones(n0), rng.normal(size=n0)])))
-    phis, alphas = np.linspace(3, 30, 50), np.linspace(0.05, 2, 20)
+        return c, X, y
 
-    def stream(rate, count):
+    def make_pred():
+        n0 = int(rng.uniform(1e3, 1e5))
+        return rng.uniform(size=(n0, 2)), np.column_stack([np.ones(n0), rng.normal(size=n0)])
+
+    datasets = [make_dataset() for _ in range(pool)]
+    preds = [make_pred() for _ in range(pool)]
+
+    def stream(rate, count, cold=False):
         t = np.cumsum(rng.exponential(1.0 / rate, size=count))
         reqs = []
         for k in range(count):
-            di, pi = int(rng.integers(pool)), int(rng.integers(pool))
-            c, X, y = datasets[di]
+            pi = int(rng.integers(pool))
             c0, X0 = preds[pi]
+            if cold:
+                c, X, y = make_dataset()
+                key = None  # its own dataset: uploaded, ordered and searched inside the request
+            else:
+                di = int(rng.integers(pool))
+                c, X, y = datasets[di]
+                key = di
             reqs.append(S.ConjRequest(c, X, y, c0, X0, float(rng.choice(phis)), float(rng.choice(alphas)),
-                                      dataset=di, rid=k, arrival=float(t[k])))
+                                      dataset=key, rid=k, arrival=float(t[k])))
         return reqs
 
-    # warm-up: every dataset resident once, kernels loaded
+    # warm-up: every pooled dataset resident once, kernels loaded
     srv = S.ConjServer(m=M, precision="fp32r", hbm_budget=150e9, ctx=ctx)
     S.serve(srv, stream(1000.0, pool), realtime=False)
     for d in range(pool):
@@ -651,6 +679,7 @@ def section_serving(sp, ctx, rates=(10, 50, 100, 200, 500), seed=55, max_request
         c0, X0 = preds[d]
         srv.submit(S.ConjRequest(c, X, y, c0, X0, 10.0, 0.5, dataset=d, rid=-1 - d))
     srv.drain()
+    S.serve(srv, stream(1000.0, 4, cold=True), realtime=False)
     # accuracy of the served (FP32R) results against FP64 on a sample
     errs = []
     for k, r in enumerate(stream(1000.0, 6)):
@@ -659,10 +688,11 @@ def section_serving(sp, ctx, rates=(10, 50, 100, 200, 500), seed=55, max_request
         ref = S.fit_predict_one(r, m=M, precision="fp64", ctx=ctx)
         errs.append(max(abs(got.ab[1] - ref.ab[1]) / abs(ref.ab[1]),
                         float(np.max(np.abs(got.y0_hat - ref.y0_hat)) / max(1.0, np.max(np.abs(ref.y0_hat))))))
-    rows = []
-    for rate in rates:
-        count = int(min(max_requests, max(40, rate * 2)))
-        reqs = stream(rate, count)
+
+    def run(rate, cold):
+        count = int(min(max_requests if not cold else 100, max(40, rate * 2)))
+        reqs = stream(rate, count, cold=cold)
+        before = dict(srv.stats)
         a = S.serve(srv, reqs)
         b = S.serve_per_request(reqs, m=M, precision="fp32r", ctx=ctx)
         # the server (one fused launch per batch) and the per-request host form run different job
@@ -675,13 +705,20 @@ def section_serving(sp, ctx, rates=(10, 50, 100, 200, 500), seed=55, max_request
                     dv = float(np.max(np.abs(u - v)) / max(1.0, float(np.max(np.abs(v)))))
                     if dv > diff:
                         diff, worst = dv, {"field": f, "rid": x.rid, "rid_other": z.rid, "batch": x.batch}
-        rows.append({"rate_rps": rate, "requests": count,
-                     "server": {k: a[k] for k in ("throughput_rps", "p50_s", "p99_s", "mean_batch", "failed")},
-                     "per_request": {k: b[k] for k in ("throughput_rps", "p50_s", "p99_s", "failed")},
-                     "max_rel_diff_server_vs_per_request": diff, "within_1e-6": diff <= 1e-6, "worst": worst})
-    return {"workload": f"Poisson streams of conjugate fit+predict requests over {pool} datasets (n log-U[1e3,5e5]) "
-                        f"and {pool} prediction sets (n0 U[1e3,1e5]), m={M}, exponential, FP32R, HBM budget 150 GB",
-            "rates": rows, "max_rel_err_fp32r_vs_fp64": float(max(errs)),
+        return {"rate_rps": rate, "requests": count,
+                "mean_n": float(np.mean([len(r.y) for r in reqs])),
+                "server": {k: a[k] for k in ("throughput_rps", "p50_s", "p99_s", "mean_batch", "failed")},
+                "per_request": {k: b[k] for k in ("throughput_rps", "p50_s", "p99_s", "failed")},
+                "dataset_builds": srv.stats["misses"] - before["misses"],
+                "max_rel_diff_server_vs_per_request": diff, "within_1e-6": diff <= 1e-6, "worst": worst}
+
+    warm = [run(rate, False) for rate in warm_rates]
+    cold = [run(rate, True) for rate in cold_rates]
+    return {"workload": f"Poisson streams of conjugate fit+predict requests, n log-U[1e3,5e5], prediction sets "
+                        f"n0 U[1e3,1e5], m={M}, exponential, FP32R, HBM budget 150 GB; warm: {pool} pooled "
+                        f"datasets kept resident; cold: a new dataset per request (upload, ordering and neighbor "
+                        f"search inside each request's latency)",
+            "warm": warm, "cold": cold, "max_rel_err_fp32r_vs_fp64": float(max(errs)),
             "server_cache": dict(srv.stats)}
 
 
@@ -983,6 +1020,34 @@ def run_profile_pass(args):
     ctx.close()
 
 
+def run_profile_rep(args):
+    """rNNGPReplicated at N locations and S samples (exponential, m = 15, FP32R), once after one
+    untimed call: a short program for ncu captures of the level-scheduled solve's kernels."""
+    import torch
+
+    import spnngp_gb300 as sp
+    from spnngp_gb300._lib import Context
+
+    n_s, ns_s = args.profile_rep.split(",")
+    n, ns = int(float(n_s)), int(ns_s)
+    ctx = Context(0)
+    c, X, _ = workload(n)
+    nb = sp.mkNNIndxCB(c, M, ctx=ctx)
+    rng = np.random.default_rng(5)
+    th = np.array(THETA)[:, None] * rng.uniform(0.8, 1.25, size=(3, ns))
+    beta = rng.normal(size=(ns, 2))
+    z = rng.standard_normal(size=n * ns)
+    run = lambda: sp.rNNGPReplicated(X, M, c, COV, nb["nnIndx"], nb["nnIndxLU"], beta, th, z,  # noqa: E731
+                                     precision="fp32r", ctx=ctx)
+    run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    y = run()["y.rep.samples"]
+    print(json.dumps({"profile_rep": args.profile_rep, "seconds": time.perf_counter() - t0,
+                      "checksum": float(np.sum(y[:, 0]))}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -993,7 +1058,7 @@ def main():
     ap.add_argument("--sections", default="config0,rep,accuracy,mcmc,conj,serve",
                     help="comma-separated extra workloads reported beside the headline (config0, rep, accuracy, "
                          "mcmc, conj, serve), or ''")
-    ap.add_argument("--mcmc-iters", type=int, default=200)
+    ap.add_argument("--mcmc-iters", type=int, default=5000)
     ap.add_argument("--launch-shape", default="",
                     help="W,G[,T]: run the FP32R register kernel with W warps per block, grid mode G and "
                          "(T = 1) the tensor-memory layout instead of the autotuned shape (results are "
@@ -1001,9 +1066,15 @@ def main():
     ap.add_argument("--profile-pass", default="",
                     help="M,MODEL,PRECISION,N: only run the fused pass at that configuration --steps times (after "
                          "one untimed call) and print its mean time -- the program for ncu captures of one kernel")
+    ap.add_argument("--profile-rep", default="",
+                    help="N,S: only run rNNGPReplicated at N locations and S samples (after one untimed call) -- "
+                         "the program for ncu captures of the replicate kernels")
     args = ap.parse_args()
     if args.profile_pass:
         run_profile_pass(args)
+        return
+    if args.profile_rep:
+        run_profile_rep(args)
         return
     args.warmup = max(args.warmup, 3)
     args.sections = [x for x in args.sections.split(",") if x]
