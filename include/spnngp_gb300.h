@@ -304,7 +304,9 @@ int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);
  * back to tuning; use_tmem is honoured for m in 11..16); nngp_autotune_report
  * writes one line per tuned class ("key: wpb=W grid_mode=G tmem=T ms=X |
  * WxBLOCKS[t]:ms ...", one entry per candidate, t marking tensor memory) into
- * buf and returns the number of classes. */
+ * buf and returns the number of classes.  The warp-per-location FP32R kernel
+ * (16 < m <= 32) is tuned the same way over 1, 2 or 4 warps per block (classes
+ * "warp M=24|32 ..."). */
 int nngp_set_autotune(nngp_ctx *ctx, int on);
 int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode, int use_tmem);
 int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len);

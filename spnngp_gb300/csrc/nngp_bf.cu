@@ -29,7 +29,9 @@ int occupancy(int wpb, int tm);
 }  // namespace nngp_bfr
 namespace nngp_bfw {
 template <int M, int MODE, int COV>
-int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1);
+int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid);
+template <int M, int MODE, int COV>
+int occupancy_warp(int wpb);
 }  // namespace nngp_bfw
 namespace nngp_bfwd {
 template <int M, int MODE, int COV>
@@ -156,22 +158,30 @@ int launch_mode(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int
   }
 }
 
-// The warp-per-location FP32R kernel (16 < m <= 32) on tiles [t0, t1)
+// The warp-per-location FP32R kernel (16 < m <= 32) on tiles [t0, t1) with wpb warps per block
+// and `grid` blocks (0: one tile per warp), or (query_occ) its blocks per SM at wpb.
+template <int M, int MODE, int COV>
+int warp_call_c(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid, bool query_occ) {
+  return query_occ ? nngp_bfw::occupancy_warp<M, MODE, COV>(wpb)
+                   : nngp_bfw::launch_warp<M, MODE, COV>(ctx, pl, t0, t1, wpb, grid);
+}
 template <int M, int MODE>
-int warp_call_m(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
-  using namespace nngp_bfw;
+int warp_call_m(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid, bool query_occ) {
   switch (pl->cov) {
-    case NNGP_COV_EXP: return launch_warp<M, MODE, NNGP_COV_EXP>(ctx, pl, t0, t1);
-    case NNGP_COV_SPH: return launch_warp<M, MODE, NNGP_COV_SPH>(ctx, pl, t0, t1);
-    case NNGP_COV_MAT_HALF: return launch_warp<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, t0, t1);
-    case NNGP_COV_GAU: return launch_warp<M, MODE, NNGP_COV_GAU>(ctx, pl, t0, t1);
-    default: return launch_warp<M, MODE, NNGP_COV_ANY>(ctx, pl, t0, t1);
+    case NNGP_COV_EXP: return warp_call_c<M, MODE, NNGP_COV_EXP>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    case NNGP_COV_SPH: return warp_call_c<M, MODE, NNGP_COV_SPH>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    case NNGP_COV_MAT_HALF: return warp_call_c<M, MODE, NNGP_COV_MAT_HALF>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    case NNGP_COV_GAU: return warp_call_c<M, MODE, NNGP_COV_GAU>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    default: return warp_call_c<M, MODE, NNGP_COV_ANY>(ctx, pl, t0, t1, wpb, grid, query_occ);
   }
 }
-int warp_call(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+int warp_call(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb = 4, int grid = 0, bool query_occ = false) {
   const bool m1 = pl->mode == 1;
-  if (pl->mmax <= 24) return m1 ? warp_call_m<24, 1>(ctx, pl, t0, t1) : warp_call_m<24, 0>(ctx, pl, t0, t1);
-  return m1 ? warp_call_m<32, 1>(ctx, pl, t0, t1) : warp_call_m<32, 0>(ctx, pl, t0, t1);
+  if (pl->mmax <= 24)
+    return m1 ? warp_call_m<24, 1>(ctx, pl, t0, t1, wpb, grid, query_occ)
+              : warp_call_m<24, 0>(ctx, pl, t0, t1, wpb, grid, query_occ);
+  return m1 ? warp_call_m<32, 1>(ctx, pl, t0, t1, wpb, grid, query_occ)
+            : warp_call_m<32, 0>(ctx, pl, t0, t1, wpb, grid, query_occ);
 }
 
 // ---------------------------------------------------------------- register kernel
@@ -325,6 +335,70 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm, t1 - t0, tm), false, t0, t1, tm);
 }
 
+// Launch shape of the warp-per-location FP32R kernel, tuned like the register kernel's: warps per
+// block 1, 2 or 4, each with one tile per warp or a persistent grid of 1 or 2 x resident blocks
+// x SMs, timed on the plan's own tiles (at most kTuneSampleTiles) on its first pass of a size
+// class; passes under stream capture or of fewer than kTuneMinTiles tiles use the tuned or the
+// default shape (4 warps, one tile per warp).
+int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  std::string key = tune_key(pl, t1 - t0);  // "M=<reg_m> ...": the warp kernel's bound instead
+  key = "warp M=" + std::to_string(pl->mmax <= 24 ? 24 : 32) + key.substr(key.find(' '));
+  auto grid_of = [&](int wpb, int gm, int ntiles) {
+    const int full = (ntiles + wpb - 1) / wpb;
+    if (gm <= 0) return full;
+    const long cap = (long)gm * warp_call(ctx, pl, 0, 0, wpb, 0, true) * (ctx->sm_count > 0 ? ctx->sm_count : 1);
+    return (int)(cap < full ? (cap > 0 ? cap : 1) : full);
+  };
+  auto it = ctx->tuned.find(key);
+  if (it == ctx->tuned.end() && ctx->autotune && t1 - t0 >= kTuneMinTiles) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(ctx->stream, &cs);
+    if (cs == cudaStreamCaptureStatusNone) {
+      const int s1 = t1 - t0 > kTuneSampleTiles ? t0 + kTuneSampleTiles : t1;
+      TuneEntry best;
+      best.ms = 1e30;
+      cudaEvent_t e0, e1;
+      NNGP_CUDA_TRY(ctx, cudaEventCreate(&e0));
+      NNGP_CUDA_TRY(ctx, cudaEventCreate(&e1));
+      int st = NNGP_OK;
+      for (int wpb : {1, 2, 4}) {
+        if (warp_call(ctx, pl, 0, 0, wpb, 0, true) <= 0) continue;
+        const int full = grid_of(wpb, 0, s1 - t0);
+        for (int gm : {0, 1, 2}) {
+          const int grid = grid_of(wpb, gm, s1 - t0);
+          if (gm > 0 && grid >= full) continue;
+          if ((st = warp_call(ctx, pl, t0, s1, wpb, grid))) break;  // warm-up
+          cudaEventRecord(e0, ctx->stream);
+          if ((st = warp_call(ctx, pl, t0, s1, wpb, grid))) break;
+          cudaEventRecord(e1, ctx->stream);
+          if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = nngp_fail(ctx, NNGP_ERR_CUDA, "autotune: event synchronisation failed");
+            break;
+          }
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          char buf[48];
+          snprintf(buf, sizeof buf, "%s%dx%d:%.4f", best.detail.empty() ? "" : " ", wpb, grid, ms);
+          best.detail += buf;
+          if (ms < best.ms) {
+            best.ms = ms;
+            best.wpb = wpb;
+            best.grid_mode = gm;
+          }
+        }
+        if (st) break;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (st) return st;
+      it = ctx->tuned.emplace(key, best).first;
+    }
+  }
+  const int wpb = it != ctx->tuned.end() ? it->second.wpb : 4;
+  const int gm = it != ctx->tuned.end() ? it->second.grid_mode : 0;
+  return warp_call(ctx, pl, t0, t1, wpb, grid_of(wpb, gm, t1 - t0));
+}
+
 // The double-float re-solve of a register-kernel plan's flagged tiles (nngp_bfdf_kernel.cuh).
 int launch_df_any(nngp_ctx *ctx, const BFPlan *pl) {
   using nngp_bfdf::launch_df;
@@ -341,7 +415,7 @@ int launch_df_any(nngp_ctx *ctx, const BFPlan *pl) {
 
 // Primary pass over tiles [t0, t1), or (fallback_pass) the FP64 re-solve of the recorded tiles.
 int launch_pass(nngp_ctx *ctx, const BFPlan *pl, bool fp32r, bool fallback_pass, int t0, int t1) {
-  if (fp32r && !fallback_pass) return pl->reg_m > 0 ? run_reg(ctx, pl, t0, t1) : warp_call(ctx, pl, t0, t1);
+  if (fp32r && !fallback_pass) return pl->reg_m > 0 ? run_reg(ctx, pl, t0, t1) : run_warp(ctx, pl, t0, t1);
   return pl->mode == 0 ? launch_mode<0>(ctx, pl, fallback_pass, t0, t1)
                        : launch_mode<1>(ctx, pl, fallback_pass, t0, t1);
 }

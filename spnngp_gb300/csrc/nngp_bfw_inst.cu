@@ -6,6 +6,8 @@
 #error "nngp_bfw_inst.cu is compiled once per variant with -DBFW_M and -DBFW_COV"
 #endif
 namespace nngp_bfw {
-template int launch_warp<BFW_M, 0, BFW_COV>(nngp_ctx *, const BFPlan *, int, int);
-template int launch_warp<BFW_M, 1, BFW_COV>(nngp_ctx *, const BFPlan *, int, int);
+template int launch_warp<BFW_M, 0, BFW_COV>(nngp_ctx *, const BFPlan *, int, int, int, int);
+template int launch_warp<BFW_M, 1, BFW_COV>(nngp_ctx *, const BFPlan *, int, int, int, int);
+template int occupancy_warp<BFW_M, 0, BFW_COV>(int);
+template int occupancy_warp<BFW_M, 1, BFW_COV>(int);
 }  // namespace nngp_bfw

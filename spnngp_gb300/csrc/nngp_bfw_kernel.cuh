@@ -341,27 +341,52 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
   }
 }
 
-constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpsPerBlock = 4;  // the largest block (the kernel's launch bounds)
+
+template <int M>
+constexpr size_t warp_smem(int wpb) {
+  return sizeof(float) * WShape<M>::WARP_FLOATS * (size_t)wpb;
+}
+
+// Raises the kernel's dynamic shared-memory limit to the largest block's (once per device).
+template <int M, int MODE, int COV>
+cudaError_t configure_warp(int device) {
+  static bool configured[64] = {};  // the attribute is per device
+  const int dev = device & 63;
+  if (configured[dev]) return cudaSuccess;
+  const cudaError_t e = cudaFuncSetAttribute(bfw_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)warp_smem<M>(kWarpsPerBlock));
+  if (e == cudaSuccess) configured[dev] = true;
+  return e;
+}
 
 // Launches the kernel on the plan's primary tiles [t0, t1) (tile = 32 locations of one job):
-// blocks of four warps (54.5 KB of shared memory at M = 32, four blocks per SM), one tile per
-// warp.
+// blocks of wpb (1 - 4) warps (54.5 KB of shared memory per four warps at M = 32), `grid`
+// blocks (0: one tile per warp; fewer: each warp loops over tiles).  Each warp reduces its own
+// tiles, so the shape never changes a result.
 template <int M, int MODE, int COV>
-int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
-  const size_t smem = sizeof(float) * WShape<M>::WARP_FLOATS * kWarpsPerBlock;
-  static bool configured[64] = {};  // the attribute is per device
-  const int dev = ctx->device & 63;
-  if (!configured[dev]) {
-    NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(bfw_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
-    configured[dev] = true;
-  }
+int launch_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid) {
+  NNGP_CUDA_TRY(ctx, (configure_warp<M, MODE, COV>(ctx->device)));
   if (t1 <= t0) return NNGP_OK;
-  const int grid = (t1 - t0 + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  bfw_kernel<M, MODE, COV><<<grid, 32 * kWarpsPerBlock, smem, ctx->stream>>>(pl->d_datas, pl->d_thetas, pl->d_jobs,
-                                                                          pl->njobs, t0, t1, pl->nv);
+  if (wpb < 1 || wpb > kWarpsPerBlock) wpb = kWarpsPerBlock;
+  const int full = (t1 - t0 + wpb - 1) / wpb;
+  if (grid <= 0 || grid > full) grid = full;
+  bfw_kernel<M, MODE, COV><<<grid, 32 * wpb, warp_smem<M>(wpb), ctx->stream>>>(pl->d_datas, pl->d_thetas,
+                                                                            pl->d_jobs, pl->njobs, t0, t1, pl->nv);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
+}
+
+// Blocks of wpb warps one SM holds at once (current device).
+template <int M, int MODE, int COV>
+int occupancy_warp(int wpb) {
+  int dev = 0, blocks = 0;
+  cudaGetDevice(&dev);
+  if (wpb < 1 || wpb > kWarpsPerBlock || configure_warp<M, MODE, COV>(dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, bfw_kernel<M, MODE, COV>, 32 * wpb,
+                                                    warp_smem<M>(wpb)) != cudaSuccess)
+    return 0;
+  return blocks;
 }
 
 }  // namespace nngp_bfw

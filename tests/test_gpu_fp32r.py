@@ -249,3 +249,29 @@ def test_double_float_tier_on_ill_conditioned_gaussian(sp, orc, m, phi):
         ld, G = sp.loglik_gram(c, o[0], o[2], m, V, "gaussian", theta, prec)
         ll[prec] = -0.5 * (ld + beta @ G[:2, :2] @ beta - 2 * beta @ G[:2, 2] + G[2, 2])
     assert abs(ll["fp32r"] - ll["fp64"]) <= 1e-6 * abs(ll["fp64"])
+
+
+@pytest.mark.parametrize("m", [20, 32])
+def test_warp_kernel_tuning_keeps_results(sp, m):
+    """The warp-per-location kernel (16 < m <= 32) is tuned on its first large pass (1, 2 or 4
+    warps per block, one tile per warp or a persistent grid); the tuned shape gives bitwise the
+    results of the default shape."""
+    c, X, y = dataset(80_000, 500 + m)
+    V = np.column_stack([X, y])
+    ctx = sp.Context(0)
+    nb = sp.mkNNIndxCB(c, m, ctx=ctx)
+    theta = (1.0, 0.1, 8.0)
+    ctx.call("nngp_set_autotune", 0)
+    B0, F0, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, "fp32r", ctx=ctx)
+    ld0, G0 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, "fp32r", ctx=ctx)
+    ctx.call("nngp_set_autotune", 1)
+    B1, F1, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, "fp32r", ctx=ctx)
+    ld1, G1 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, "fp32r", ctx=ctx)
+    rep = ctx.autotune_report()
+    keys = [k for k in rep if k.startswith(f"warp M={24 if m <= 24 else 32} ")]
+    assert len(keys) == 2  # the standalone and the fused mode
+    for k in keys:
+        assert rep[k]["wpb"] in (1, 2, 4) and len(rep[k]["candidates"]) >= 3
+    assert np.array_equal(B0, B1) and np.array_equal(F0, F1)
+    assert ld0 == ld1 and np.array_equal(G0, G1)
+    ctx.close()
