@@ -254,3 +254,21 @@ def test_bad_arguments_raise(sp):
                     (1, 0.1, 1), "fp64")
     with pytest.raises(ValueError):
         sp.cov_model_index("cubic")
+
+
+def test_fp64_pass_on_two_devices_in_one_process(sp, orc):
+    """The FP64 kernels' shared-memory attribute is set per device: a pass on a second device of
+    the same process must launch (skipped when only one GPU is visible)."""
+    import torch
+
+    if torch.cuda.device_count() < 2:
+        pytest.skip("one GPU visible")
+    rng = np.random.default_rng(9)
+    c = xorder(rng.uniform(size=(3000, 2)))
+    o = orc.mkNNIndxCB(cm(c), 15)
+    out = []
+    for dev in (0, 1):
+        ctx = sp.Context(dev)
+        out.append(sp.updateBF(c, o[0], o[2], 15, "exponential", (1.0, 0.1, 6.0), "fp64", ctx=ctx))
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
