@@ -282,10 +282,10 @@ int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations);
 
 /* Precision diagnostic, no counterpart in the reference: how the locations
  * counted by nngp_fp32r_resolved were re-solved -- in double-float arithmetic
- * on the FP32 pipe (neighbor bounds m <= 16: the flagged locations of the
- * register kernel go there first) or in FP64 (every flagged location for
- * 16 < m <= 32; for m <= 16 the 64-location tiles holding a location the
- * double-float solve could not certify).  Synchronises the context's stream. */
+ * on the FP32 pipe (every flagged location goes there first: a thread per
+ * location for m <= 16, a warp per location beyond) or in FP64 (the tiles, 64
+ * locations for m <= 16 and 32 beyond, holding a location the double-float
+ * solve could not certify).  Synchronises the context's stream. */
 int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);
 
 /* Launch-shape autotuner of the FP32R B/F kernel for m <= 16, no counterpart

@@ -41,6 +41,10 @@ namespace nngp_bfdf {
 template <int MODE, int COV>
 int launch_df(nngp_ctx *ctx, const BFPlan *pl);
 }  // namespace nngp_bfdf
+namespace nngp_bfwdf {
+template <int M, int MODE, int COV>
+int launch_wdf(nngp_ctx *ctx, const BFPlan *pl);
+}  // namespace nngp_bfwdf
 using namespace nngp_bf;
 
 namespace {
@@ -399,9 +403,26 @@ int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   return warp_call(ctx, pl, t0, t1, wpb, grid_of(wpb, gm, t1 - t0));
 }
 
-// The double-float re-solve of a register-kernel plan's flagged tiles (nngp_bfdf_kernel.cuh).
+// The warp-per-location double-float re-solve (nngp_bfwdf_kernel.cuh) for 16 < m <= 32.
+template <int M>
+int launch_wdf_m(nngp_ctx *ctx, const BFPlan *pl) {
+  using nngp_bfwdf::launch_wdf;
+  const bool fused = pl->mode == 1;
+  switch (pl->cov) {
+    case NNGP_COV_EXP: return fused ? launch_wdf<M, 1, NNGP_COV_EXP>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_EXP>(ctx, pl);
+    case NNGP_COV_SPH: return fused ? launch_wdf<M, 1, NNGP_COV_SPH>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_SPH>(ctx, pl);
+    case NNGP_COV_MAT_HALF:
+      return fused ? launch_wdf<M, 1, NNGP_COV_MAT_HALF>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_MAT_HALF>(ctx, pl);
+    case NNGP_COV_GAU: return fused ? launch_wdf<M, 1, NNGP_COV_GAU>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_GAU>(ctx, pl);
+    default: return fused ? launch_wdf<M, 1, NNGP_COV_ANY>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_ANY>(ctx, pl);
+  }
+}
+
+// The double-float re-solve of an FP32R plan's flagged tiles: thread per location for the
+// register kernel's bounds (nngp_bfdf_kernel.cuh), warp per location beyond.
 int launch_df_any(nngp_ctx *ctx, const BFPlan *pl) {
   using nngp_bfdf::launch_df;
+  if (pl->reg_m == 0) return pl->mmax <= 24 ? launch_wdf_m<24>(ctx, pl) : launch_wdf_m<32>(ctx, pl);
   const bool fused = pl->mode == 1;
   switch (pl->cov) {
     case NNGP_COV_EXP: return fused ? launch_df<1, NNGP_COV_EXP>(ctx, pl) : launch_df<0, NNGP_COV_EXP>(ctx, pl);
@@ -490,15 +511,11 @@ int nngp_bf_plan(nngp_ctx *ctx, BFPlan *pl, int precision, int mode, int nv,
     pl->d_fb_words = (unsigned *)own(sizeof(unsigned) * (1 + (size_t)pl->tiles_fb));
     pl->d_fb_list = (int *)own(sizeof(int) * (size_t)(pl->tiles_fb > 0 ? pl->tiles_fb : 1));
     if (!pl->d_fb_words || !pl->d_fb_list) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
-    if (pl->reg_m > 0) {  // flagged tiles: double-float kernel first, then FP64 for what it cannot certify
-      pl->d_fb64_list = (int *)own(sizeof(int) * (size_t)(pl->tiles_fb > 0 ? pl->tiles_fb : 1));
-      pl->d_fb64_locs = (unsigned long long *)own(2 * sizeof(unsigned long long));
-      if (!pl->d_fb64_list || !pl->d_fb64_locs) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
-      pl->d_fb64_count = reinterpret_cast<int *>(pl->d_fb64_locs + 1);
-    } else {
-      pl->d_fb64_list = pl->d_fb_list;
-      pl->d_fb64_count = (int *)pl->d_fb_words;
-    }
+    // flagged tiles: double-float kernel first, then FP64 for the tiles it cannot certify
+    pl->d_fb64_list = (int *)own(sizeof(int) * (size_t)(pl->tiles_fb > 0 ? pl->tiles_fb : 1));
+    pl->d_fb64_locs = (unsigned long long *)own(2 * sizeof(unsigned long long));
+    if (!pl->d_fb64_list || !pl->d_fb64_locs) return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
+    pl->d_fb64_count = reinterpret_cast<int *>(pl->d_fb64_locs + 1);
     size_t fb = 0;
     for (const PassEval &e : evals) fb += (size_t)datas[e.data].n;
     pl->flags_bytes = fb;
@@ -597,7 +614,7 @@ int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   const bool fp32r = pl->precision == NNGP_FP32R;
   // FP32R: the re-solve of the recorded tiles (register-kernel plans: double-float first, FP64
   // for the tiles it cannot certify), folded into the same fixed-order sums
-  if (fp32r && pl->reg_m > 0 && (st = launch_df_any(ctx, pl))) return st;
+  if (fp32r && (st = launch_df_any(ctx, pl))) return st;
   if (fp32r && (st = launch_pass(ctx, pl, false, true, 0, 0))) return st;
   reduce_chunks_kernel<<<pl->njobs * pl->red_chunks, 256, 0, ctx->stream>>>(
       pl->d_jobs, fp32r ? pl->d_jobs_fb : nullptr, fp32r ? pl->d_fb_words + 1 : nullptr,

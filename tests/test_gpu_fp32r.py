@@ -222,13 +222,14 @@ def test_resolved_count_reports_fp64_handoffs(sp, orc, m):
     assert ctx.fp32r_resolved() == (0, 0)
 
 
-@pytest.mark.parametrize("m", [10, 15, 16])
+@pytest.mark.parametrize("m", [10, 15, 16, 20, 32])
 @pytest.mark.parametrize("phi", [34.62, 3.462])
 def test_double_float_tier_on_ill_conditioned_gaussian(sp, orc, m, phi):
     """Gaussian covariance with a 1e-6 nugget (condition numbers ~1e7): nearly every location is
-    flagged by the float solve; the double-float re-solve takes them (FP64 only for tiles it
-    cannot certify), and F stays within 1e-6 of its exact value (extended precision) and the
-    log-likelihood within 1e-6 of the FP64 form."""
+    flagged by the float solve; the double-float re-solve takes them (thread per location for
+    m <= 16, warp per location beyond; FP64 only for tiles it cannot certify), and F stays
+    within 1e-6 of its exact value (extended precision) and the log-likelihood within 1e-6 of
+    the FP64 form."""
     from test_gpu_parity_scale import _exact_F
 
     c, X, y = dataset(4000, 300 + m)
