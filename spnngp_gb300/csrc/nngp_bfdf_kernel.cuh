@@ -8,44 +8,85 @@
 // nngp_cov_df.cuh):
 //   1. neighbor offsets from the split coordinates as double-float pairs on a common grid
 //      (as the register kernel), the covariance c and the lower triangle of C in double-float;
-//   2. the row-oriented (Banachiewicz) Cholesky factor L in double-float with the forward
-//      solve z = L^-1 c fused in, then F = sigma^2 + tau^2 - z'z (the squared norm of the
-//      forward solve, accurate where F is a small difference) and B = L^-T z;
+//   2. the Cholesky factor of the augmented matrix [C c; c' S] (S = sigma^2 + tau^2) in
+//      double-float, right-looking (outer-product form): its last row is z = L^-1 c and its
+//      last pivot is F = S - z'z, the quantity NNGP needs (accurate where F is a small
+//      difference); then B = L^-T z by the same outer-product form run backwards;
 //   3. log F and, in the fused pass, r = (I - B) V and r_a r_b / F in FP64 (a few dozen FP64
 //      operations per location), summed over the tile in a fixed order.
-// Every dot product runs as two independent sums (even and odd terms) and the covariance
-// entries are evaluated two at a time, so consecutive double-float operations seldom wait on
-// each other: the kernel holds only about four warps per SM (its triangles fill the shared
-// memory), and latency, not arithmetic, bounds it.
+// The right-looking form leaves every update of a step independent of the others.  With its
+// triangles filling the shared memory the kernel holds only four warps per SM, so the
+// independence has to show within a thread: every loop issues a batch of loads (four updates,
+// four rows, two covariance pairs), then the arithmetic, then the stores -- a store to shared
+// memory holds back the next iteration's loads otherwise, since the compiler cannot tell the
+// indices apart.  Rows are stored as float pairs (k, k + 1), each row of the lower triangle
+// with its diagonal padded to an even length, so one 64-bit shared load brings two entries and
+// one packed f32x2 instruction updates both (a - l b with the hi product carried exactly by
+// an fma, the cross terms rounded below 2^-23 of the product); the covariance entries are
+// evaluated two at a time.  (A row-by-row factorization with compensated dot products issued
+// about one instruction at a time; fully unrolling the factorization per neighbor bound cut
+// the instruction count by 40 % but overflowed the instruction cache.)
 // The kernel walks the FP32R pass's list of flagged FP64 tiles (64 locations each, the FP64
 // kernel's tile) and solves every flagged location of a tile.  A location it cannot certify --
 // a non-positive double-float pivot, F < 1e-6 (sigma^2 + tau^2), or a squared pivot ratio (a
 // lower bound of the condition number) above 1e10 -- sends its whole tile on to the FP64
 // kernel (a second list), so every tile's partial sums come from one kernel and keep their
-// fixed order.  Each thread keeps its triangle in shared memory, element e of thread t at
-// e * TPB + t (hi and lo parts in separate arrays), so every access is bank-conflict free.
+// fixed order.  Each thread keeps its matrix in shared memory, pair p of thread t at
+// p * TPB + t (hi and lo parts in separate arrays), so every access is bank-conflict free.
 #pragma once
 #include <cuda_runtime.h>
 #include "nngp_cov_df.cuh"
 
 namespace nngp_bfdf {
 
-constexpr int M = 16;    // the register kernel's largest neighbor bound
-constexpr int TPB = 64;  // the FP64 tile of m <= 16 (the unit of the flagged-tile list)
-constexpr int NT = M * (M + 1) / 2;
+constexpr int M = 16;      // the register kernel's largest neighbor bound
+constexpr int MA = M + 1;  // rows of the augmented matrix
+constexpr int TPB = 64;    // the FP64 tile of m <= 16 (the unit of the flagged-tile list)
 constexpr int kNGMax = 1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2;
-// floats per thread: L hi and lo (NT each), z / c hi and lo (M each), geometry (4 M)
-constexpr int kThreadFloats = 2 * NT + 2 * M + 4 * M;
-constexpr size_t kSmemBytes = sizeof(float) * ((size_t)kThreadFloats * TPB + (TPB / 32) * nngp_bfr::kTabFloats) +
+// Row r (entries 0 .. r, padded to an even count) starts at pair (r + 1)^2 / 4.
+__host__ __device__ constexpr int row_pair0(int r) { return (r + 1) * (r + 1) / 4; }
+constexpr int NP = row_pair0(MA);  // pairs of the augmented triangle
+constexpr int NCP = (MA + 1) / 2;  // pairs of the column buffer (entries 0 .. MA)
+// shared memory per thread (bytes): triangle hi and lo pairs, column hi and lo pairs, geometry
+constexpr int kThreadBytes = 8 * (2 * NP + 2 * NCP) + 16 * MA;
+constexpr size_t kSmemBytes = (size_t)kThreadBytes * TPB + sizeof(float) * (TPB / 32) * nngp_bfr::kTabFloats +
                               sizeof(double) * (TPB / 32) * kNGMax;
+static_assert(2 * (kSmemBytes + 1024) <= 228 * 1024, "two blocks per SM");
 constexpr float kMaxPivotRatio2 = 1e10f;  // squared pivot ratio above which FP64 takes over
-
-__host__ __device__ constexpr int tri(int r, int c) { return r * (r + 1) / 2 + c; }  // c <= r
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+using nngp_df2::p2;
+
+// a - l b on both halves for double-float a, l, b, given nl = -l (normalised result): the hi
+// parts' sum exact (two_sum), the product of the hi parts exact (fma), the cross terms rounded
+// (below 2^-23 of the product)
+__device__ __forceinline__ void fms(p2 &ah, p2 &al, p2 lh, p2 nlh, p2 nll, p2 bh, p2 bl) {
+  namespace G = nngp_df2;
+  const p2 pn = G::mul(nlh, bh);     // -(lh bh) rounded
+  const p2 pe = G::fma(lh, bh, pn);  // its rounding error, exactly
+  const p2 t = G::fma(nlh, bl, G::fma(nll, bh, G::sub(al, pe)));
+  p2 s, e;
+  G::two_sum(ah, pn, s, e);
+  G::fast_two_sum(s, G::add(e, t), ah, al);
+}
+
+// sigma^2 rho for two squared distances (double-float), packed where the model allows
+template <int COV>
+__device__ __forceinline__ nngp_df2::df2 cov_two(nngp_df2::df2 d2, const nngp_bfr::CorDF &ck, const float *tab,
+                                                 const CovParams *cp) {
+  namespace G = nngp_df2;
+  if constexpr (nngp_bfr::kPacked<COV>) {
+    return nngp_bfr::cov_df2<COV>(d2, ck, tab);
+  } else {
+    const nngp_df::df a = nngp_bfr::cov_df<COV>(nngp_df::df{G::first(d2.h), G::first(d2.l)}, ck, tab, cp);
+    const nngp_df::df b = nngp_bfr::cov_df<COV>(nngp_df::df{G::second(d2.h), G::second(d2.l)}, ck, tab, cp);
+    return G::df2{G::pack(a.h, b.h), G::pack(a.l, b.l)};
+  }
 }
 
 template <int MODE, int COV>
@@ -56,17 +97,17 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
                                                  int *__restrict__ list64, int *__restrict__ count64,
                                                  unsigned long long *__restrict__ locs64) {
   namespace F = nngp_df;
+  namespace G = nngp_df2;
   extern __shared__ __align__(16) float smem_d[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  float *Lh = smem_d, *Ll = Lh + NT * TPB;
-  float *zh = Ll + NT * TPB, *zl = zh + M * TPB;
-  float4 *geo = reinterpret_cast<float4 *>(zl + M * TPB);
-  float *tab = smem_d + (size_t)kThreadFloats * TPB + warp * nngp_bfr::kTabFloats;
-  double *wbuf = reinterpret_cast<double *>(smem_d + (size_t)kThreadFloats * TPB + (TPB / 32) * nngp_bfr::kTabFloats);
-#define LH(r, c) Lh[tri(r, c) * TPB + tid]
-#define LL(r, c) Ll[tri(r, c) * TPB + tid]
-#define ZH(k) zh[(k) * TPB + tid]
-#define ZL(k) zl[(k) * TPB + tid]
+  p2 *Ah = reinterpret_cast<p2 *>(smem_d), *Al = Ah + NP * TPB;
+  p2 *Ch = Al + NP * TPB, *Cl = Ch + NCP * TPB;
+  float4 *geo = reinterpret_cast<float4 *>(Cl + NCP * TPB);
+  float *tab = reinterpret_cast<float *>(geo + MA * TPB) + warp * nngp_bfr::kTabFloats;
+  double *wbuf = reinterpret_cast<double *>(reinterpret_cast<float *>(geo + MA * TPB) + (TPB / 32) * nngp_bfr::kTabFloats);
+  // pair q of a pair array, and element k (of the pairs starting at q0) as a float
+#define PR(a, q) a[(q) * TPB + tid]
+#define EL(a, q0, k) reinterpret_cast<float *>(&a[((q0) + ((k) >> 1)) * TPB + tid])[(k) & 1]
 #define GEO(k) geo[(k) * TPB + tid]
 
   const int ntodo = *tile_count;
@@ -90,115 +131,187 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
     bool ok = true;
     F::df Fd{1.0f, 0.0f};
     if (active) {
-      // ---- 1. geometry and covariance (double-float)
+      // ---- 1. geometry (the location itself last, at the origin) and the augmented matrix.
+      // Every loop below issues a batch of independent loads, then the arithmetic, then the
+      // stores: a store to shared memory would otherwise hold back the next iteration's loads
+      // (the compiler cannot tell the indices apart) and leave one instruction in flight.
       const float4 *xyf = reinterpret_cast<const float4 *>(d.xyf);
       const float4 pi4 = xyf[i];
+      int nb[M];
+#pragma unroll
+      for (int k = 0; k < M; k++) nb[k] = k < mi ? d.nnIndx[off + k] : i;
+      float4 g[M];
       float omax = 1e-30f;
-      for (int k = 0; k < mi; k++) {
-        const float4 q = xyf[d.nnIndx[off + k]];
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float4 q = xyf[nb[k]];
         const F::df ox = F::diff(q.x, q.z, pi4.x, pi4.z), oy = F::diff(q.y, q.w, pi4.y, pi4.w);
-        GEO(k) = make_float4(ox.h, oy.h, ox.l, oy.l);
-        omax = fmaxf(omax, fmaxf(fabsf(ox.h), fabsf(oy.h)));
+        g[k] = make_float4(ox.h, oy.h, ox.l, oy.l);
+        omax = fmaxf(omax, fmaxf(fabsf(ox.h), fabsf(oy.h)));  // zero past m_i (nb = i)
       }
       // hi parts on a common grid 2^e >= 2^-22 max |offset|: two hi parts subtract exactly
       const int eb = ((__float_as_int(omax) >> 23) & 0xff) - 22;
       const float grid = __int_as_float(max(eb, 1) << 23), inv = __int_as_float((254 - max(eb, 1)) << 23);
-      for (int k = 0; k < mi; k++) {
-        const float4 g = GEO(k);
-        const float hx = __fmul_rn(rintf(__fmul_rn(g.x, inv)), grid);
-        const float hy = __fmul_rn(rintf(__fmul_rn(g.y, inv)), grid);
-        const float4 q = make_float4(hx, hy, __fadd_rn(__fsub_rn(g.x, hx), g.z), __fadd_rn(__fsub_rn(g.y, hy), g.w));
-        GEO(k) = q;
-        const F::df gx = F::norm(q.x, q.z), gy = F::norm(q.y, q.w);
-        const F::df c = nngp_bfr::cov_df<COV>(F::sumsq(gx.h, gx.l, gy.h, gy.l), ck, tab, cpp);
-        ZH(k) = c.h;
-        ZL(k) = c.l;
+#pragma unroll
+      for (int k = 0; k < M; k++) {
+        const float hx = __fmul_rn(rintf(__fmul_rn(g[k].x, inv)), grid);
+        const float hy = __fmul_rn(rintf(__fmul_rn(g[k].y, inv)), grid);
+        if (k < mi)
+          GEO(k) = make_float4(hx, hy, __fadd_rn(__fsub_rn(g[k].x, hx), g[k].z), __fadd_rn(__fsub_rn(g[k].y, hy), g[k].w));
       }
-      // the strict lower triangle two entries at a time (independent evaluations interleave)
-      for (int r = 0; r < mi; r++) {
+      GEO(mi) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      // row r: C_r0 .. C_r,r-1 and S (row mi: c' and S), four entries per step; an even row
+      // ends in the pair (S, 0)
+      PR(Ah, 0) = G::pack(Sd.h, 0.0f);
+      PR(Al, 0) = G::pack(Sd.l, 0.0f);
+      for (int r = 1; r <= mi; r++) {
+        const int fr = row_pair0(r);
         const float4 gr = GEO(r);
-        for (int c = 0; c < r; c += 2) {
-          const int c1 = c + 1 < r ? c + 1 : c;
-          const float4 ga = GEO(c), gb = GEO(c1);
-          F::df ax, ay, bx, by;
-          F::fast_two_sum(__fsub_rn(gr.x, ga.x), __fsub_rn(gr.z, ga.z), ax.h, ax.l);
-          F::fast_two_sum(__fsub_rn(gr.y, ga.y), __fsub_rn(gr.w, ga.w), ay.h, ay.l);
-          F::fast_two_sum(__fsub_rn(gr.x, gb.x), __fsub_rn(gr.z, gb.z), bx.h, bx.l);
-          F::fast_two_sum(__fsub_rn(gr.y, gb.y), __fsub_rn(gr.w, gb.w), by.h, by.l);
-          const F::df va = nngp_bfr::cov_df<COV>(F::sumsq(ax.h, ax.l, ay.h, ay.l), ck, tab, cpp);
-          const F::df vb = nngp_bfr::cov_df<COV>(F::sumsq(bx.h, bx.l, by.h, by.l), ck, tab, cpp);
-          LH(r, c) = va.h;
-          LL(r, c) = va.l;
-          LH(r, c1) = vb.h;  // c1 == c on an odd row end: the same value again
-          LL(r, c1) = vb.l;
-        }
-        LH(r, r) = Sd.h;
-        LL(r, r) = Sd.l;
-      }
-      // ---- 2. Cholesky (row by row) with z = L^-1 c; the diagonal slots end holding 1 / L_rr
-      float pmin = 3.4e38f, pmax = 0.0f;
-      F::df zz{0.0f, 0.0f};
-      for (int r = 0; r < mi && ok; r++) {
-        for (int c = 0; c < r; c++) {
-          F::df s0{0.0f, 0.0f}, s1{0.0f, 0.0f};
-          int k = 0;
-          for (; k + 1 < c; k += 2) {
-            s0 = F::add(s0, F::mul(F::df{LH(r, k), LL(r, k)}, F::df{LH(c, k), LL(c, k)}));
-            s1 = F::add(s1, F::mul(F::df{LH(r, k + 1), LL(r, k + 1)}, F::df{LH(c, k + 1), LL(c, k + 1)}));
+        const p2 grx = G::splat(gr.x), gry = G::splat(gr.y), grz = G::splat(gr.z), grw = G::splat(gr.w);
+        for (int c = 0; c < r; c += 4) {
+          const float4 a0 = GEO(c), a1 = GEO(min(c + 1, r - 1)), b0 = GEO(min(c + 2, r - 1)), b1 = GEO(min(c + 3, r - 1));
+          G::df2 ex, ey, fx, fy;
+          G::fast_two_sum(G::sub(grx, G::pack(a0.x, a1.x)), G::sub(grz, G::pack(a0.z, a1.z)), ex.h, ex.l);
+          G::fast_two_sum(G::sub(gry, G::pack(a0.y, a1.y)), G::sub(grw, G::pack(a0.w, a1.w)), ey.h, ey.l);
+          G::fast_two_sum(G::sub(grx, G::pack(b0.x, b1.x)), G::sub(grz, G::pack(b0.z, b1.z)), fx.h, fx.l);
+          G::fast_two_sum(G::sub(gry, G::pack(b0.y, b1.y)), G::sub(grw, G::pack(b0.w, b1.w)), fy.h, fy.l);
+          const G::df2 va = cov_two<COV>(G::sumsq(ex, ey), ck, tab, cpp);
+          const G::df2 vb = cov_two<COV>(G::sumsq(fx, fy), ck, tab, cpp);
+          const int q = fr + (c >> 1);
+          PR(Ah, q) = c + 1 < r ? va.h : G::pack(G::first(va.h), Sd.h);
+          PR(Al, q) = c + 1 < r ? va.l : G::pack(G::first(va.l), Sd.l);
+          if (c + 2 < r) {
+            PR(Ah, q + 1) = c + 3 < r ? vb.h : G::pack(G::first(vb.h), Sd.h);
+            PR(Al, q + 1) = c + 3 < r ? vb.l : G::pack(G::first(vb.l), Sd.l);
           }
-          if (k < c) s0 = F::add(s0, F::mul(F::df{LH(r, k), LL(r, k)}, F::df{LH(c, k), LL(c, k)}));
-          const F::df s = F::sub(F::df{LH(r, c), LL(r, c)}, F::add(s0, s1));
-          const F::df l = F::mul(s, F::df{LH(c, c), LL(c, c)});  // times 1 / L_cc
-          LH(r, c) = l.h;
-          LL(r, c) = l.l;
         }
-        F::df d0{0.0f, 0.0f}, d1{0.0f, 0.0f}, z0{0.0f, 0.0f}, z1{0.0f, 0.0f};
-        int k = 0;
-        for (; k + 1 < r; k += 2) {
-          const F::df la{LH(r, k), LL(r, k)}, lb{LH(r, k + 1), LL(r, k + 1)};
-          d0 = F::add(d0, F::mul(la, la));
-          d1 = F::add(d1, F::mul(lb, lb));
-          z0 = F::add(z0, F::mul(la, F::df{ZH(k), ZL(k)}));
-          z1 = F::add(z1, F::mul(lb, F::df{ZH(k + 1), ZL(k + 1)}));
+        if (!(r & 1)) {
+          PR(Ah, fr + (r >> 1)) = G::pack(Sd.h, 0.0f);
+          PR(Al, fr + (r >> 1)) = G::pack(Sd.l, 0.0f);
         }
-        if (k < r) {
-          const F::df la{LH(r, k), LL(r, k)};
-          d0 = F::add(d0, F::mul(la, la));
-          z0 = F::add(z0, F::mul(la, F::df{ZH(k), ZL(k)}));
-        }
-        const F::df dg = F::sub(F::df{LH(r, r), LL(r, r)}, F::add(d0, d1));
-        F::df zr = F::sub(F::df{ZH(r), ZL(r)}, F::add(z0, z1));
-        ok = dg.h > 0.0f;
-        if (!ok) break;
-        const F::df lrr = F::sqrt(dg);
-        pmin = fminf(pmin, lrr.h);
-        pmax = fmaxf(pmax, lrr.h);
-        const F::df ir = F::recip(lrr);
-        LH(r, r) = ir.h;
-        LL(r, r) = ir.l;
-        zr = F::mul(zr, ir);
-        ZH(r) = zr.h;
-        ZL(r) = zr.l;
-        zz = F::add(zz, F::mul(zr, zr));
       }
+#pragma unroll
+      for (int q = 0; q < NCP; q++) PR(Ch, q) = PR(Cl, q) = 0;
+      // ---- 2. right-looking Cholesky of the augmented matrix; the diagonal slots end holding
+      // 1 / L_KK, row mi ends holding z and, on its diagonal, F
+      float pmin = 3.4e38f, pmax = 0.0f;
+      for (int K = 0; K < mi; K++) {
+        const int fk = row_pair0(K);
+        const F::df dK = F::norm(EL(Ah, fk, K), EL(Al, fk, K));
+        ok = dK.h > 0.0f;
+        if (!ok) break;
+        const F::df lkk = F::sqrt(dK);
+        pmin = fminf(pmin, lkk.h);
+        pmax = fmaxf(pmax, lkk.h);
+        const F::df ik = F::recip(lkk);
+        EL(Ah, fk, K) = ik.h;
+        EL(Al, fk, K) = ik.l;
+        EL(Ch, 0, K) = 0.0f;  // the update below leaves column K itself alone
+        EL(Cl, 0, K) = 0.0f;
+        // column K of L, also into the column buffer, four rows per step
+        for (int r0 = K + 1; r0 <= mi; r0 += 4) {
+          float xh[4], xl[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int fr = row_pair0(min(r0 + u, mi));
+            xh[u] = EL(Ah, fr, K);
+            xl[u] = EL(Al, fr, K);
+          }
+          F::df l[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) l[u] = F::mul(F::df{xh[u], xl[u]}, ik);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int r = r0 + u;
+            if (r <= mi) {
+              const int fr = row_pair0(r);
+              EL(Ah, fr, K) = l[u].h;
+              EL(Al, fr, K) = l[u].l;
+              EL(Ch, 0, r) = l[u].h;
+              EL(Cl, 0, r) = l[u].l;
+            }
+          }
+        }
+        // A_rj -= L_rK L_jK for K < j <= r <= mi: pairs (r, q), q from the one holding K + 1
+        // to the one holding r, walked four at a time in row order
+        const int q0 = (K + 1) >> 1;
+        int r = K + 1, q = q0;
+        while (r <= mi) {
+          int at[4], cq[4], cr[4];
+          bool on[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            on[u] = r <= mi;
+            cr[u] = min(r, mi);
+            cq[u] = min(q, cr[u] >> 1);
+            at[u] = row_pair0(cr[u]) + cq[u];
+            if (++q > (r >> 1)) {
+              r++;
+              q = q0;
+            }
+          }
+          p2 ah[4], al[4], bh[4], bl[4], lh[4], nlh[4], nll[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            ah[u] = PR(Ah, at[u]);
+            al[u] = PR(Al, at[u]);
+            bh[u] = PR(Ch, cq[u]);
+            bl[u] = PR(Cl, cq[u]);
+            const float xh = EL(Ch, 0, cr[u]), xl = EL(Cl, 0, cr[u]);
+            lh[u] = G::splat(xh);
+            nlh[u] = G::splat(-xh);
+            nll[u] = G::splat(-xl);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) fms(ah[u], al[u], lh[u], nlh[u], nll[u], bh[u], bl[u]);
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (on[u]) {
+              PR(Ah, at[u]) = ah[u];
+              PR(Al, at[u]) = al[u];
+            }
+        }
+      }
+      const int fz = row_pair0(mi);
       if (ok) {
-        Fd = F::sub(Sd, zz);
+        Fd = F::norm(EL(Ah, fz, mi), EL(Al, fz, mi));
         const float ratio = pmax / pmin;
         ok = Fd.h > nngp_bfr::kMinFRel * Sd.h && ratio * ratio <= kMaxPivotRatio2;
       }
       if (ok) {
-        // ---- B = L^-T z (in place of z)
-        for (int k = mi - 1; k >= 0; k--) {
-          F::df b0{0.0f, 0.0f}, b1{0.0f, 0.0f};
-          int r = k + 1;
-          for (; r + 1 < mi; r += 2) {
-            b0 = F::add(b0, F::mul(F::df{LH(r, k), LL(r, k)}, F::df{ZH(r), ZL(r)}));
-            b1 = F::add(b1, F::mul(F::df{LH(r + 1, k), LL(r + 1, k)}, F::df{ZH(r + 1), ZL(r + 1)}));
+        // ---- B = L^-T z in place of z: b_r = z_r / L_rr, then z_k -= L_rk b_r for k < r
+        for (int r = mi - 1; r >= 0; r--) {
+          const int fr = row_pair0(r);
+          const F::df b = F::mul(F::df{EL(Ah, fz, r), EL(Al, fz, r)}, F::df{EL(Ah, fr, r), EL(Al, fr, r)});
+          EL(Ah, fz, r) = b.h;
+          EL(Al, fz, r) = b.l;
+          const p2 bh = G::splat(b.h), nbh = G::splat(-b.h), nbl = G::splat(-b.l);
+          const int nq = r >> 1;
+          for (int q0 = 0; q0 < nq; q0 += 4) {
+            p2 zh[4], zl[4], xh[4], xl[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int q = min(q0 + u, nq - 1);
+              zh[u] = PR(Ah, fz + q);
+              zl[u] = PR(Al, fz + q);
+              xh[u] = PR(Ah, fr + q);
+              xl[u] = PR(Al, fr + q);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) fms(zh[u], zl[u], bh, nbh, nbl, xh[u], xl[u]);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+              if (q0 + u < nq) {
+                PR(Ah, fz + q0 + u) = zh[u];
+                PR(Al, fz + q0 + u) = zl[u];
+              }
           }
-          if (r < mi) b0 = F::add(b0, F::mul(F::df{LH(r, k), LL(r, k)}, F::df{ZH(r), ZL(r)}));
-          const F::df b = F::mul(F::sub(F::df{ZH(k), ZL(k)}, F::add(b0, b1)), F::df{LH(k, k), LL(k, k)});
-          ZH(k) = b.h;
-          ZL(k) = b.l;
+          if (r & 1) {  // entry r - 1 opens the pair that ends on the diagonal
+            const F::df z = F::sub(F::df{EL(Ah, fz, r - 1), EL(Al, fz, r - 1)},
+                                   F::mul(b, F::df{EL(Ah, fr, r - 1), EL(Al, fr, r - 1)}));
+            EL(Ah, fz, r - 1) = z.h;
+            EL(Al, fz, r - 1) = z.l;
+          }
         }
       }
     }
@@ -213,18 +326,19 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
       continue;
     }
     // ---- 3. log F and the likelihood terms in FP64, tile sums in a fixed order
+    const int fz = row_pair0(mi);
     const double Fi = F::to_double(Fd);
     double logF = 0.0;
     double rv[NNGP_MAX_NV] = {};
     if (active) {
       logF = log(Fi);
       if (MODE == 0) {
-        for (int k = 0; k < mi; k++) d.B[off + k] = (double)ZH(k) + (double)ZL(k);
+        for (int k = 0; k < mi; k++) d.B[off + k] = (double)EL(Ah, fz, k) + (double)EL(Al, fz, k);
         d.F[i] = Fi;
       } else {
         for (int v = 0; v < nv; v++) rv[v] = d.V[(size_t)i * nv + v];
         for (int k = 0; k < mi; k++) {
-          const double bk = (double)ZH(k) + (double)ZL(k);
+          const double bk = (double)EL(Ah, fz, k) + (double)EL(Al, fz, k);
           const double *vrow = d.V + (size_t)d.nnIndx[off + k] * nv;
           for (int v = 0; v < nv; v++) rv[v] = fma(-bk, vrow[v], rv[v]);
         }
@@ -260,10 +374,8 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
     }
     __syncthreads();
   }
-#undef LH
-#undef LL
-#undef ZH
-#undef ZL
+#undef PR
+#undef EL
 #undef GEO
 }
 
