@@ -283,7 +283,7 @@ int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations);
 /* Precision diagnostic, no counterpart in the reference: how the locations
  * counted by nngp_fp32r_resolved were re-solved -- in double-float arithmetic
  * on the FP32 pipe (every flagged location goes there first: a thread per
- * location for m <= 16, a warp per location beyond) or in FP64 (the tiles, 64
+ * location for m <= 24, a warp per location beyond) or in FP64 (the tiles, 64
  * locations for m <= 16 and 32 beyond, holding a location the double-float
  * solve could not certify).  Synchronises the context's stream. */
 int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);

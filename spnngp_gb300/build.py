@@ -30,7 +30,8 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 # (FP64: the shared-memory kernel of nngp_bf_inst.cu for m <= 24, the warp-per-location
 # kernel of nngp_bfwd_inst.cu for 24 < m <= 32; FP32R: the register kernel of nngp_bfr_inst.cu
 # for m <= 16, the warp-per-location kernel of nngp_bfw_inst.cu for 16 < m <= 32, and the
-# double-float re-solves of their flagged locations, nngp_bfdf_inst.cu and nngp_bfwdf_inst.cu)
+# double-float re-solves of their flagged locations: thread per location for bounds 16 and 24,
+# nngp_bfdf_inst.cu, warp per location for 32, nngp_bfwdf_inst.cu)
 VARIANTS = {
     "nngp_bf_inst.cu": [(f"_m{m}_c{c}", [f"-DBF_M={m}", f"-DBF_COV={c}"])
                         for m in (16, 24) for c in (0, 1, 2, 3, 4)],
@@ -40,9 +41,10 @@ VARIANTS = {
                          for m in (10, 15, 16) for c in (0, 1, 2, 3, 4)],
     "nngp_bfw_inst.cu": [(f"_m{m}_c{c}", [f"-DBFW_M={m}", f"-DBFW_COV={c}"])
                          for m in (24, 32) for c in (0, 1, 2, 3, 4)],
-    "nngp_bfdf_inst.cu": [(f"_c{c}", [f"-DBFDF_COV={c}"]) for c in (0, 1, 2, 3, 4)],
+    "nngp_bfdf_inst.cu": [(f"_m{m}_c{c}", [f"-DBFDF_M={m}", f"-DBFDF_COV={c}"])
+                          for m in (16, 24) for c in (0, 1, 2, 3, 4)],
     "nngp_bfwdf_inst.cu": [(f"_m{m}_c{c}", [f"-DBFWDF_M={m}", f"-DBFWDF_COV={c}"])
-                           for m in (24, 32) for c in (0, 1, 2, 3, 4)],
+                           for m in (32,) for c in (0, 1, 2, 3, 4)],
 }
 
 

@@ -38,7 +38,7 @@ template <int M, int MODE, int COV>
 int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
 }  // namespace nngp_bfwd
 namespace nngp_bfdf {
-template <int MODE, int COV>
+template <int M, int MODE, int COV>
 int launch_df(nngp_ctx *ctx, const BFPlan *pl);
 }  // namespace nngp_bfdf
 namespace nngp_bfwdf {
@@ -403,35 +403,39 @@ int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   return warp_call(ctx, pl, t0, t1, wpb, grid_of(wpb, gm, t1 - t0));
 }
 
-// The warp-per-location double-float re-solve (nngp_bfwdf_kernel.cuh) for 16 < m <= 32.
 template <int M>
-int launch_wdf_m(nngp_ctx *ctx, const BFPlan *pl) {
+int launch_df_m(nngp_ctx *ctx, const BFPlan *pl) {
+  using nngp_bfdf::launch_df;
+  const bool fused = pl->mode == 1;
+  switch (pl->cov) {
+    case NNGP_COV_EXP: return fused ? launch_df<M, 1, NNGP_COV_EXP>(ctx, pl) : launch_df<M, 0, NNGP_COV_EXP>(ctx, pl);
+    case NNGP_COV_SPH: return fused ? launch_df<M, 1, NNGP_COV_SPH>(ctx, pl) : launch_df<M, 0, NNGP_COV_SPH>(ctx, pl);
+    case NNGP_COV_MAT_HALF:
+      return fused ? launch_df<M, 1, NNGP_COV_MAT_HALF>(ctx, pl) : launch_df<M, 0, NNGP_COV_MAT_HALF>(ctx, pl);
+    case NNGP_COV_GAU: return fused ? launch_df<M, 1, NNGP_COV_GAU>(ctx, pl) : launch_df<M, 0, NNGP_COV_GAU>(ctx, pl);
+    default: return fused ? launch_df<M, 1, NNGP_COV_ANY>(ctx, pl) : launch_df<M, 0, NNGP_COV_ANY>(ctx, pl);
+  }
+}
+int launch_wdf_32(nngp_ctx *ctx, const BFPlan *pl) {
   using nngp_bfwdf::launch_wdf;
   const bool fused = pl->mode == 1;
   switch (pl->cov) {
-    case NNGP_COV_EXP: return fused ? launch_wdf<M, 1, NNGP_COV_EXP>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_EXP>(ctx, pl);
-    case NNGP_COV_SPH: return fused ? launch_wdf<M, 1, NNGP_COV_SPH>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_SPH>(ctx, pl);
+    case NNGP_COV_EXP: return fused ? launch_wdf<32, 1, NNGP_COV_EXP>(ctx, pl) : launch_wdf<32, 0, NNGP_COV_EXP>(ctx, pl);
+    case NNGP_COV_SPH: return fused ? launch_wdf<32, 1, NNGP_COV_SPH>(ctx, pl) : launch_wdf<32, 0, NNGP_COV_SPH>(ctx, pl);
     case NNGP_COV_MAT_HALF:
-      return fused ? launch_wdf<M, 1, NNGP_COV_MAT_HALF>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_MAT_HALF>(ctx, pl);
-    case NNGP_COV_GAU: return fused ? launch_wdf<M, 1, NNGP_COV_GAU>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_GAU>(ctx, pl);
-    default: return fused ? launch_wdf<M, 1, NNGP_COV_ANY>(ctx, pl) : launch_wdf<M, 0, NNGP_COV_ANY>(ctx, pl);
+      return fused ? launch_wdf<32, 1, NNGP_COV_MAT_HALF>(ctx, pl) : launch_wdf<32, 0, NNGP_COV_MAT_HALF>(ctx, pl);
+    case NNGP_COV_GAU: return fused ? launch_wdf<32, 1, NNGP_COV_GAU>(ctx, pl) : launch_wdf<32, 0, NNGP_COV_GAU>(ctx, pl);
+    default: return fused ? launch_wdf<32, 1, NNGP_COV_ANY>(ctx, pl) : launch_wdf<32, 0, NNGP_COV_ANY>(ctx, pl);
   }
 }
 
-// The double-float re-solve of an FP32R plan's flagged tiles: thread per location for the
-// register kernel's bounds (nngp_bfdf_kernel.cuh), warp per location beyond.
+// The double-float re-solve of an FP32R plan's flagged tiles: thread per location for bounds
+// 16 and 24 (nngp_bfdf_kernel.cuh; the flagged-tile list's tile is the FP64 kernel's, 64
+// locations up to 16 neighbors and 32 beyond), warp per location for 32 (nngp_bfwdf_kernel.cuh:
+// a thread-per-location triangle of that size leaves one 32-thread block per SM).
 int launch_df_any(nngp_ctx *ctx, const BFPlan *pl) {
-  using nngp_bfdf::launch_df;
-  if (pl->reg_m == 0) return pl->mmax <= 24 ? launch_wdf_m<24>(ctx, pl) : launch_wdf_m<32>(ctx, pl);
-  const bool fused = pl->mode == 1;
-  switch (pl->cov) {
-    case NNGP_COV_EXP: return fused ? launch_df<1, NNGP_COV_EXP>(ctx, pl) : launch_df<0, NNGP_COV_EXP>(ctx, pl);
-    case NNGP_COV_SPH: return fused ? launch_df<1, NNGP_COV_SPH>(ctx, pl) : launch_df<0, NNGP_COV_SPH>(ctx, pl);
-    case NNGP_COV_MAT_HALF:
-      return fused ? launch_df<1, NNGP_COV_MAT_HALF>(ctx, pl) : launch_df<0, NNGP_COV_MAT_HALF>(ctx, pl);
-    case NNGP_COV_GAU: return fused ? launch_df<1, NNGP_COV_GAU>(ctx, pl) : launch_df<0, NNGP_COV_GAU>(ctx, pl);
-    default: return fused ? launch_df<1, NNGP_COV_ANY>(ctx, pl) : launch_df<0, NNGP_COV_ANY>(ctx, pl);
-  }
+  if (pl->mmax <= 16) return launch_df_m<16>(ctx, pl);
+  return pl->mmax <= 24 ? launch_df_m<24>(ctx, pl) : launch_wdf_32(ctx, pl);
 }
 
 // Primary pass over tiles [t0, t1), or (fallback_pass) the FP64 re-solve of the recorded tiles.

@@ -39,19 +39,26 @@
 
 namespace nngp_bfdf {
 
-constexpr int M = 16;      // the register kernel's largest neighbor bound
-constexpr int MA = M + 1;  // rows of the augmented matrix
-constexpr int TPB = 64;    // the FP64 tile of m <= 16 (the unit of the flagged-tile list)
 constexpr int kNGMax = 1 + NNGP_MAX_NV * (NNGP_MAX_NV + 1) / 2;
 // Row r (entries 0 .. r, padded to an even count) starts at pair (r + 1)^2 / 4.
 __host__ __device__ constexpr int row_pair0(int r) { return (r + 1) * (r + 1) / 4; }
-constexpr int NP = row_pair0(MA);  // pairs of the augmented triangle
-constexpr int NCP = (MA + 1) / 2;  // pairs of the column buffer (entries 0 .. MA)
-// shared memory per thread (bytes): triangle hi and lo pairs, column hi and lo pairs, geometry
-constexpr int kThreadBytes = 8 * (2 * NP + 2 * NCP) + 16 * MA;
-constexpr size_t kSmemBytes = (size_t)kThreadBytes * TPB + sizeof(float) * (TPB / 32) * nngp_bfr::kTabFloats +
-                              sizeof(double) * (TPB / 32) * kNGMax;
-static_assert(2 * (kSmemBytes + 1024) <= 228 * 1024, "two blocks per SM");
+// The kernel for neighbor bound M (16 or 24): a block is one FP64 tile (the unit of the
+// flagged-tile list: 64 locations for m <= 16, 32 beyond), a thread one location; the
+// augmented matrix has M + 1 rows.  Shared memory per thread: the triangle's hi and lo pairs,
+// the column buffer's hi and lo pairs (entries 0 .. M + 1), the geometry (a float4 per row).
+template <int M>
+struct Shape {
+  static constexpr int TPB = M <= 16 ? 64 : 32;
+  static constexpr int MA = M + 1;
+  static constexpr int NP = row_pair0(MA);
+  static constexpr int NCP = (MA + 1) / 2;
+  static constexpr int kThreadBytes = 8 * (2 * NP + 2 * NCP) + 16 * MA;
+  static constexpr size_t kSmemBytes = (size_t)kThreadBytes * TPB +
+                                       sizeof(float) * (TPB / 32) * nngp_bfr::kTabFloats +
+                                       sizeof(double) * (TPB / 32) * kNGMax;
+  static constexpr int kBlocksPerSM = (int)((228 * 1024) / (kSmemBytes + 1024));  // 2 at M = 16 and 24
+  static_assert(kSmemBytes <= 227 * 1024 && kBlocksPerSM >= 1, "one block per SM at least");
+};
 constexpr float kMaxPivotRatio2 = 1e10f;  // squared pivot ratio above which FP64 takes over
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -89,8 +96,8 @@ __device__ __forceinline__ nngp_df2::df2 cov_two(nngp_df2::df2 d2, const nngp_bf
   }
 }
 
-template <int MODE, int COV>
-__global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ datas,
+template <int M, int MODE, int COV>
+__global__ void __launch_bounds__(Shape<M>::TPB) bfdf_kernel(const BFData *__restrict__ datas,
                                                  const CovParams *__restrict__ thetas,
                                                  const BFJob *__restrict__ jobs_fb, int njobs, int nv,
                                                  const int *__restrict__ tile_list, const int *__restrict__ tile_count,
@@ -98,6 +105,8 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
                                                  unsigned long long *__restrict__ locs64) {
   namespace F = nngp_df;
   namespace G = nngp_df2;
+  using S = Shape<M>;
+  constexpr int TPB = S::TPB, MA = S::MA, NP = S::NP, NCP = S::NCP;
   extern __shared__ __align__(16) float smem_d[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   p2 *Ah = reinterpret_cast<p2 *>(smem_d), *Al = Ah + NP * TPB;
@@ -137,27 +146,37 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
       // (the compiler cannot tell the indices apart) and leave one instruction in flight.
       const float4 *xyf = reinterpret_cast<const float4 *>(d.xyf);
       const float4 pi4 = xyf[i];
-      int nb[M];
-#pragma unroll
-      for (int k = 0; k < M; k++) nb[k] = k < mi ? d.nnIndx[off + k] : i;
-      float4 g[M];
       float omax = 1e-30f;
+      for (int k0 = 0; k0 < mi; k0 += 8) {  // eight gathers in flight
+        int nb[8];
 #pragma unroll
-      for (int k = 0; k < M; k++) {
-        const float4 q = xyf[nb[k]];
-        const F::df ox = F::diff(q.x, q.z, pi4.x, pi4.z), oy = F::diff(q.y, q.w, pi4.y, pi4.w);
-        g[k] = make_float4(ox.h, oy.h, ox.l, oy.l);
-        omax = fmaxf(omax, fmaxf(fabsf(ox.h), fabsf(oy.h)));  // zero past m_i (nb = i)
+        for (int u = 0; u < 8; u++) nb[u] = k0 + u < mi ? d.nnIndx[off + k0 + u] : i;
+        float4 q[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) q[u] = xyf[nb[u]];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const F::df ox = F::diff(q[u].x, q[u].z, pi4.x, pi4.z), oy = F::diff(q[u].y, q[u].w, pi4.y, pi4.w);
+          omax = fmaxf(omax, fmaxf(fabsf(ox.h), fabsf(oy.h)));  // zero past m_i (nb = i)
+          if (k0 + u < mi) GEO(k0 + u) = make_float4(ox.h, oy.h, ox.l, oy.l);
+        }
       }
       // hi parts on a common grid 2^e >= 2^-22 max |offset|: two hi parts subtract exactly
       const int eb = ((__float_as_int(omax) >> 23) & 0xff) - 22;
       const float grid = __int_as_float(max(eb, 1) << 23), inv = __int_as_float((254 - max(eb, 1)) << 23);
+      for (int k0 = 0; k0 < mi; k0 += 4) {
+        float4 g[4];
 #pragma unroll
-      for (int k = 0; k < M; k++) {
-        const float hx = __fmul_rn(rintf(__fmul_rn(g[k].x, inv)), grid);
-        const float hy = __fmul_rn(rintf(__fmul_rn(g[k].y, inv)), grid);
-        if (k < mi)
-          GEO(k) = make_float4(hx, hy, __fadd_rn(__fsub_rn(g[k].x, hx), g[k].z), __fadd_rn(__fsub_rn(g[k].y, hy), g[k].w));
+        for (int u = 0; u < 4; u++) g[u] = GEO(min(k0 + u, mi - 1));
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const float hx = __fmul_rn(rintf(__fmul_rn(g[u].x, inv)), grid);
+          const float hy = __fmul_rn(rintf(__fmul_rn(g[u].y, inv)), grid);
+          g[u] = make_float4(hx, hy, __fadd_rn(__fsub_rn(g[u].x, hx), g[u].z), __fadd_rn(__fsub_rn(g[u].y, hy), g[u].w));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (k0 + u < mi) GEO(k0 + u) = g[u];
       }
       GEO(mi) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       // row r: C_r0 .. C_r,r-1 and S (row mi: c' and S), four entries per step; an even row
@@ -379,21 +398,22 @@ __global__ void __launch_bounds__(TPB) bfdf_kernel(const BFData *__restrict__ da
 #undef GEO
 }
 
-// Walks the plan's flagged-tile list with about two blocks per SM; tiles it cannot certify are
-// appended to the plan's FP64 list.
-template <int MODE, int COV>
+// Walks the plan's flagged-tile list with as many blocks as the SMs hold at once (one tile per
+// block); tiles it cannot certify are appended to the plan's FP64 list.
+template <int M, int MODE, int COV>
 int launch_df(nngp_ctx *ctx, const BFPlan *pl) {
+  using S = Shape<M>;
   static bool configured[64] = {};  // the attribute is per device
   const int dev = ctx->device & 63;
   if (!configured[dev]) {
-    NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(bfdf_kernel<MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)kSmemBytes));
+    NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(bfdf_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)S::kSmemBytes));
     configured[dev] = true;
   }
   if (pl->tiles_fb <= 0) return NNGP_OK;
-  const int cap = 2 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
+  const int cap = S::kBlocksPerSM * (ctx->sm_count > 0 ? ctx->sm_count : 1);
   const int grid = pl->tiles_fb < cap ? pl->tiles_fb : cap;
-  bfdf_kernel<MODE, COV><<<grid, TPB, kSmemBytes, ctx->stream>>>(
+  bfdf_kernel<M, MODE, COV><<<grid, S::TPB, S::kSmemBytes, ctx->stream>>>(
       pl->d_datas, pl->d_thetas, pl->d_jobs_fb, pl->njobs, pl->nv, pl->d_fb_list, (const int *)pl->d_fb_words,
       pl->d_fb64_list, pl->d_fb64_count, pl->d_fb64_locs);
   NNGP_LAUNCH_CHECK(ctx);

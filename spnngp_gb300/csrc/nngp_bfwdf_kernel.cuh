@@ -1,8 +1,9 @@
-// Double-float re-solve of the locations the warp-per-location FP32R kernel (16 < m <= 32,
+// Double-float re-solve of the locations the warp-per-location FP32R kernel (24 < m <= 32,
 // nngp_bfw_kernel.cuh) flags -- typically a gaussian covariance with a small nugget, whose
-// float factor cannot be certified.  A thread-per-location triangle at this bound would need
-// ~5 KB of shared memory per thread, so this kernel keeps the warp-per-location layout of the
-// FP32R kernel and factors in double-float arithmetic on the FP32 pipe instead of handing the
+// float factor cannot be certified.  A thread-per-location triangle at this bound needs
+// ~5.4 KB of shared memory per thread (one 32-thread block per SM; the thread-per-location
+// kernel of nngp_bfdf_kernel.cuh serves m <= 24), so this kernel keeps the warp-per-location
+// layout of the FP32R kernel and factors in double-float arithmetic on the FP32 pipe instead of handing the
 // locations to the FP64 kernel (reference updateBF, src/rNNGP.cpp:46-101, and the likelihood
 // sums of src/rNNGP.cpp:306-317):
 //   1. geometry and the covariance in double-float exactly as the FP32R warp kernel builds it
