@@ -382,13 +382,15 @@ ACCURACY_CASES = [("exponential", 0.05, (1.0, 0.1, 59.91)), ("exponential", 0.5,
                   ("gaussian", 0.05, (1.0, 1e-6, 34.62)), ("gaussian", 0.5, (1.0, 1e-6, 3.462))]
 
 
-def section_accuracy(sp, ctx, dev, n=N, ms=(15, 32), seed=2024, reps=3):
+def section_accuracy(sp, ctx, dev, n=N, ms=(15, 20, 32), seed=2024, reps=3):
     """Plain method at scale, FP64 vs FP32 + refinement: n = 1e6 uniform locations, the code-book
     neighbor search, then one updateBF and one fused log-likelihood at fixed theta for each
     model and range; errors of the FP32R form against the FP64 form (itself pinned to the oracle
     to 1e-10 by the tests), the time of the whole fused pass (device-resident inputs; FP32R:
-    primary kernel, FP64 re-solve of the flagged locations and the sums) after one untimed call
-    (which also tunes a new kernel class), and how many locations the FP32R pass re-solved."""
+    primary kernel, the double-float and FP64 re-solves of the flagged locations, the sums)
+    after one untimed call (which also tunes a new kernel class), and how many locations the
+    FP32R pass re-solved in each tier.  m = 15 runs the register kernel, 20 and 32 the
+    warp-per-location kernel (bounds 24 and 32)."""
     import torch
 
     from spnngp_gb300._lib import _dp

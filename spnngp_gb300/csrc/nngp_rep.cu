@@ -14,8 +14,7 @@
 //   level_kernel    lev[i] = 1 + max lev[N(i)] (lev[0] = 0).  Blocks take tickets in the
 //                   order they start, so a location waits only on locations of blocks that
 //                   are resident or done; each wait on a neighbor's level is bounded (an
-//                   error flag and an early return after kSpinLimit polls), and polls
-//                   without sleeping (the critical path is the DAG's depth);
+//                   error flag and an early return after kSpinLimit polls);
 //   level_count / level_scatter   a counting sort of the locations by level (order within
 //                   a level is arbitrary: the locations of one level do not read each other).
 // Per chunk of samples: the standalone B/F pass at every sample's parameter set (the same
@@ -31,7 +30,7 @@
 
 namespace {
 
-constexpr int kSpinLimit = 1 << 22;  // polls of one neighbor's level (an L2 round trip each)
+constexpr int kSpinLimit = 1 << 21;  // polls of one neighbor's level (each >= 64 ns apart)
 
 __device__ __forceinline__ int ld_relaxed(const int *p) {
   int v;
@@ -61,11 +60,13 @@ __global__ void level_kernel(int n, const int *__restrict__ nnIndx, const int *_
     }
     int v = ld_relaxed(lev + k);
     int spins = 0;
-    while (v < 0) {  // plain polling: a sleep between polls lengthened every level of the DAG's critical path
+    while (v < 0) {  // a short sleep between polls: polling flat out from every waiting thread
+                     // crowds the memory system and slowed each level of the critical path
       if (++spins > kSpinLimit) {
         atomicOr(err, 2);
         break;
       }
+      __nanosleep(64);
       v = ld_relaxed(lev + k);
     }
     if (v >= l) l = v + 1;
