@@ -514,7 +514,7 @@ def section_config0(sp, ctx, skip_cpu=False):
 def section_replicate(sp, ctx, n=N, n_samples=100, skip_cpu=False, seed=404):
     """Replicated data (rNNGPReplicated, the y_rep of fit.rep / fitted.NNGP) at n = 1e6, m = 15,
     exponential, n_samples parameter sets scattered around the headline theta: the
-    level-scheduled GPU solve through the public call (host data in and out), FP32R and FP64,
+    dataflow GPU solve through the public call (host data in and out), FP32R and FP64,
     against the oracle's sequential recurrence on a two-sample slice of the same inputs."""
     rng = np.random.default_rng(seed)
     c, X, _ = workload(n)
@@ -1024,7 +1024,7 @@ def run_profile_pass(args):
 
 def run_profile_rep(args):
     """rNNGPReplicated at N locations and S samples (exponential, m = 15, FP32R), once after one
-    untimed call: a short program for ncu captures of the level-scheduled solve's kernels."""
+    untimed call: a short program for ncu captures of the replicate solve's kernels."""
     import torch
 
     import spnngp_gb300 as sp

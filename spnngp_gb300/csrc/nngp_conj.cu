@@ -454,7 +454,7 @@ int nngp_rNNGPReplicated(nngp_ctx *ctx, const double *X, int p, int n, int m, co
   nngp_prepare_coords(ctx, dcm, n, xy, xyf);
   int st = nngp_reset_status(ctx, dst);
   if (st) return st;
-  // the level-scheduled solve of every sample's recurrence (nngp_rep.cu)
+  // the dataflow solve of every sample's recurrence (nngp_rep.cu)
   RepSpec rs{};
   rs.n = n;
   rs.m = m;

@@ -19,7 +19,7 @@
 // (fit.rep, src/rNNGP.cpp:300-303,309-313) records the current theta, the beta
 // draw and where its n normals start in the stream; the draws do not feed back
 // into the chain, so after the last iteration all of them are made at once by
-// the level-scheduled solve of nngp_rep.cu (the recurrence of
+// the dataflow solve of nngp_rep.cu (the recurrence of
 // src/rNNGP.cpp:24-42 for every recorded theta).
 // Random numbers come from host-fed streams in the reference's order.  Each
 // iteration is captured once as a CUDA graph and replayed.
@@ -517,7 +517,7 @@ int nngp_run_mcmc(nngp_ctx *ctx, const std::vector<MCInstance> &insts, int preci
       if (states[k].status == 3) st = nngp_fail(ctx, NNGP_ERR_STREAM, "rNNGP: a host-fed random stream ran out");
     }
   }
-  // the recorded replicate draws, every one of an instance in one level-scheduled solve
+  // the recorded replicate draws, every one of an instance in one dataflow solve
   for (int k = 0; k < ninst && !st; k++) {
     const MCConst &c = consts[k];
     if (!c.repTheta || states[k].repCnt == 0) continue;

@@ -1,26 +1,25 @@
-// Replicated data by a level-scheduled sparse triangular solve.
+// Replicated data by a dataflow sparse triangular solve.
 //
 // The reference draws one replicate v at parameter set s by the sequential recurrence
 //   v_0 = sqrt(F_0) z_0,   v_i = B_i . v_N(i) + sqrt(F_i) z_i    (i = 1 .. n-1)
 // (updateRep, src/rNNGP.cpp:24-42, and the per-sample loop of src/rNNGPReplicated.cpp:
 // 183-205), then y_rep = X beta_s + v.  That is the unit lower-triangular solve
 // (I - B) v = F^(1/2) z, sequential only along the neighbor DAG: v_i waits for its m
-// neighbors, nothing else.  Its depth is about 8.5 sqrt(n) for x-ordered uniform locations
-// (8,454 levels at n = 1e6, ~118 locations per level), so the solve runs one launch per
-// level over every (location in the level) x (sample) pair of a chunk of samples, instead of
-// one thread walking all n locations per sample.
+// neighbors, nothing else.  The DAG's depth is about 8.5 sqrt(n) for x-ordered uniform
+// locations (8,454 levels at n = 1e6, ~118 locations per level on average).
 //
-// The level schedule is built once per neighbor structure on the device:
-//   level_kernel    lev[i] = 1 + max lev[N(i)] (lev[0] = 0).  Blocks take tickets in the
-//                   order they start, so a location waits only on locations of blocks that
-//                   are resident or done; each wait on a neighbor's level is bounded (an
-//                   error flag and an early return after kSpinLimit polls);
-//   level_count / level_scatter   a counting sort of the locations by level (order within
-//                   a level is arbitrary: the locations of one level do not read each other).
-// Per chunk of samples: the standalone B/F pass at every sample's parameter set (the same
-// kernels as updateBF), the level launches, then y_rep = X beta + v in the reference's
-// summation order (rNNGPReplicated: v, then + beta_j X_ij for j in order, as dgemv does;
-// the response MCMC: X beta first, then + v, as its dgemv / daxpy do).
+// rep_flow_kernel solves a chunk of samples in one launch without a level schedule: each warp
+// takes the next location from a ticket counter (locations in index order, a topological
+// order of the DAG since every neighbor precedes its location; for x-ordered data it is
+// also close to level order), waits until its neighbors are published, computes v_i for
+// every sample of the chunk (lane t: samples t, t + 32, ...), and publishes location i.  A
+// location waits only on smaller tickets, held by warps already running, so the waits always
+// end; each is bounded all the same (kSpinLimit polls, then an error bit; the host fails the
+// call).  v is read through L2 only: an SM's L1 may hold a line from before another SM wrote
+// it.  Per chunk of samples: the standalone B/F pass at every sample's parameter set (the
+// same kernels as updateBF), the solve, then y_rep = X beta + v in the reference's summation
+// order (rNNGPReplicated: v, then + beta_j X_ij for j in order, as dgemv does; the response
+// MCMC: X beta first, then + v, as its dgemv / daxpy do).
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstring>
@@ -30,65 +29,20 @@
 
 namespace {
 
-constexpr int kSpinLimit = 1 << 21;  // polls of one neighbor's level (each >= 64 ns apart)
+constexpr int kSpinLimit = 1 << 21;  // polls of one neighbor's flag (each >= 32 ns apart)
 
-__device__ __forceinline__ int ld_relaxed(const int *p) {
+__device__ __forceinline__ int ld_acquire(const int *p) {
   int v;
-  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_relaxed(int *p, int v) {
-  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// err bit 1: a neighbor index that is not a predecessor (k < 0 or k >= i); bit 2: a wait ran
-// out of polls.  lev must hold -1 everywhere on entry; depth receives 1 + the largest level.
-__global__ void level_kernel(int n, const int *__restrict__ nnIndx, const int *__restrict__ nnLU, int *lev,
-                             unsigned *ticket, int *err, int *depth) {
-  __shared__ unsigned blk;
-  if (threadIdx.x == 0) blk = atomicAdd(ticket, 1u);
-  __syncthreads();
-  const long long i = (long long)blk * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int off = nnLU[i], cnt = nnLU[n + i];
-  int l = 0;
-  for (int j = 0; j < cnt; j++) {
-    const int k = nnIndx[off + j];
-    if (k < 0 || k >= i) {
-      atomicOr(err, 1);
-      continue;
-    }
-    int v = ld_relaxed(lev + k);
-    int spins = 0;
-    while (v < 0) {  // a short sleep between polls: polling flat out from every waiting thread
-                     // crowds the memory system and slowed each level of the critical path
-      if (++spins > kSpinLimit) {
-        atomicOr(err, 2);
-        break;
-      }
-      __nanosleep(64);
-      v = ld_relaxed(lev + k);
-    }
-    if (v >= l) l = v + 1;
-  }
-  st_relaxed(lev + i, l);
-  atomicMax(depth, l + 1);
-}
-
-__global__ void level_count_kernel(int n, const int *__restrict__ lev, int *__restrict__ count) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) atomicAdd(count + lev[i], 1);
-}
-
-__global__ void level_scatter_kernel(int n, const int *__restrict__ lev, int *__restrict__ cursor,
-                                     int *__restrict__ order) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) order[atomicAdd(cursor + lev[i], 1)] = (int)i;
+__device__ __forceinline__ void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 struct LevelArgs {
   int n, ns, r0;
-  const int *nnIndx, *nnLU, *order;
+  const int *nnIndx, *nnLU;
   const double *B;  // ns x nI: sample t's packed B at B + t nI
   int64_t nI;
   const double *F;  // ns x n
@@ -97,21 +51,55 @@ struct LevelArgs {
   double *vbuf;     // n x ns, location-major (the ns samples of a location are contiguous)
 };
 
-// Locations order[lo .. lo + cnt) of one level, every sample of the chunk: thread (q, t),
-// t fastest, so the samples of a neighbor are read as one contiguous run.  The sum is the
-// reference's ddot order (j = 0 .. cnt - 1) without fused multiply-adds.
-__global__ void rep_level_kernel(LevelArgs a, int lo, int cnt) {
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= (long long)cnt * a.ns) return;
-  const int t = (int)(tid % a.ns);
-  const int i = a.order[lo + (int)(tid / a.ns)];
-  const double *Bt = a.B + (size_t)t * a.nI;
-  const int off = a.nnLU[i], c = a.nnLU[a.n + i];
-  double acc = 0.0;
-  for (int j = 0; j < c; j++)
-    acc = __dadd_rn(acc, __dmul_rn(Bt[off + j], a.vbuf[(size_t)a.nnIndx[off + j] * a.ns + t]));
-  const double zz = a.z[a.zoff[a.r0 + t] + i];
-  a.vbuf[(size_t)i * a.ns + t] = __dadd_rn(acc, __dmul_rn(sqrt(a.F[(size_t)t * a.n + i]), zz));
+// words[0]: the ticket counter; words[1]: error bits (1: a neighbor that is not a
+// predecessor, 2: a wait ran out of polls); ready[i] != 0 once v_i of every sample is written.
+// The sum is the reference's ddot order (j = 0 .. cnt - 1) without fused multiply-adds.
+constexpr int kFlowWarps = 4;  // warps per block
+
+__global__ void __launch_bounds__(32 * kFlowWarps) rep_flow_kernel(LevelArgs a, int *ready, int *words) {
+  __shared__ int nbs[kFlowWarps][32];  // the current location's neighbors, per warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int *ticket = words, *err = words + 1;
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(ticket, 1);
+    const int i = __shfl_sync(0xffffffffu, k, 0);
+    if (i >= a.n) break;
+    const int off = a.nnLU[i], c = a.nnLU[a.n + i];
+    int nb = 0;
+    if (lane < c) {  // c <= 32: one neighbor per lane
+      nb = a.nnIndx[off + lane];
+      if (nb < 0 || nb >= i) {
+        atomicOr(err, 1);
+        nb = 0;
+      } else {
+        int spins = 0;
+        while (ld_acquire(ready + nb) == 0) {
+          if (++spins > kSpinLimit) {
+            atomicOr(err, 2);
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+    }
+    if (lane < c) nbs[warp][lane] = nb;
+    __syncwarp();
+    for (int t = lane; t < a.ns; t += 32) {
+      const double *Bt = a.B + (size_t)t * a.nI + off;
+      double acc = 0.0;
+      for (int j = 0; j < c; j++)
+        acc = __dadd_rn(acc, __dmul_rn(Bt[j], __ldcg(a.vbuf + (size_t)nbs[warp][j] * a.ns + t)));
+      const double zz = a.z[a.zoff[a.r0 + t] + i];
+      a.vbuf[(size_t)i * a.ns + t] = __dadd_rn(acc, __dmul_rn(sqrt(a.F[(size_t)t * a.n + i]), zz));
+    }
+    __syncwarp();  // every lane's stores precede the flag; nbs is rewritten next round
+    if (lane == 0) {
+      __threadfence();
+      st_release(ready + i, 1);
+    }
+    __syncwarp();
+  }
 }
 
 // y_rep of sample r0 + t at location i (i fastest: coalesced writes).
@@ -132,81 +120,12 @@ long long nblocks(long long work, int tpb) { return (work + tpb - 1) / tpb; }
 
 }  // namespace
 
-int nngp_level_schedule(nngp_ctx *ctx, int n, const int *nnIndx, const int *nnLU, LevelSchedule *ls) {
-  ls->n = n;
-  ls->depth = 0;
-  ls->start.clear();
-  ls->order = (int *)nngp_malloc_async(ctx, sizeof(int) * (size_t)n);
-  int *lev = (int *)nngp_malloc_async(ctx, sizeof(int) * (size_t)n);
-  int *words = (int *)nngp_malloc_async(ctx, sizeof(int) * 4);  // ticket, err, depth
-  if (!ls->order || !lev || !words) {
-    nngp_free_async(ctx, ls->order);
-    nngp_free_async(ctx, lev);
-    nngp_free_async(ctx, words);
-    ls->order = nullptr;
-    return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
-  }
-  auto done = [&](int st) {
-    nngp_free_async(ctx, lev);
-    nngp_free_async(ctx, words);
-    if (st) {
-      nngp_free_async(ctx, ls->order);
-      ls->order = nullptr;
-    }
-    return st;
-  };
-  if (cudaMemsetAsync(lev, 0xFF, sizeof(int) * (size_t)n, ctx->stream) != cudaSuccess ||
-      cudaMemsetAsync(words, 0, sizeof(int) * 4, ctx->stream) != cudaSuccess)
-    return done(nngp_fail(ctx, NNGP_ERR_CUDA, "level schedule: memset failed"));
-  level_kernel<<<(unsigned)nblocks(n, 128), 128, 0, ctx->stream>>>(n, nnIndx, nnLU, lev, (unsigned *)words,
-                                                                    words + 1, words + 2);
-  ctx->launches++;
-  int h[4] = {};
-  cudaMemcpyAsync(h, words, sizeof(int) * 4, cudaMemcpyDeviceToHost, ctx->stream);
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  if (e != cudaSuccess)
-    return done(nngp_fail(ctx, NNGP_ERR_CUDA, std::string("level schedule: ") + cudaGetErrorString(e)));
-  if (h[1] & 1) return done(nngp_fail(ctx, NNGP_ERR_ARG, "nnIndx lists a neighbor that is not a predecessor"));
-  if (h[1] & 2) return done(nngp_fail(ctx, NNGP_ERR_CUDA, "level schedule: a wait for a neighbor's level timed out"));
-  const int depth = h[2];
-  int *count = (int *)nngp_malloc_async(ctx, sizeof(int) * (size_t)(depth + 1));
-  if (!count) return done(nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed"));
-  cudaMemsetAsync(count, 0, sizeof(int) * (size_t)(depth + 1), ctx->stream);
-  level_count_kernel<<<(unsigned)nblocks(n, 256), 256, 0, ctx->stream>>>(n, lev, count);
-  ctx->launches++;
-  std::vector<int> hc(depth + 1, 0);
-  cudaMemcpyAsync(hc.data(), count, sizeof(int) * (size_t)depth, cudaMemcpyDeviceToHost, ctx->stream);
-  e = cudaStreamSynchronize(ctx->stream);
-  if (e != cudaSuccess) {
-    nngp_free_async(ctx, count);
-    return done(nngp_fail(ctx, NNGP_ERR_CUDA, std::string("level schedule: ") + cudaGetErrorString(e)));
-  }
-  ls->start.assign(depth + 1, 0);
-  for (int l = 0; l < depth; l++) ls->start[l + 1] = ls->start[l] + hc[l];
-  cudaMemcpyAsync(count, ls->start.data(), sizeof(int) * (size_t)depth, cudaMemcpyHostToDevice, ctx->stream);
-  level_scatter_kernel<<<(unsigned)nblocks(n, 256), 256, 0, ctx->stream>>>(n, lev, count, ls->order);
-  ctx->launches++;
-  e = cudaStreamSynchronize(ctx->stream);  // the host start vector is read by the copy above
-  nngp_free_async(ctx, count);
-  if (e != cudaSuccess) return done(nngp_fail(ctx, NNGP_ERR_CUDA, std::string("level schedule: ") + cudaGetErrorString(e)));
-  ls->depth = depth;
-  return done(NNGP_OK);
-}
-
-void nngp_level_schedule_free(nngp_ctx *ctx, LevelSchedule *ls) {
-  nngp_free_async(ctx, ls->order);
-  ls->order = nullptr;
-  ls->start.clear();
-  ls->depth = 0;
-}
-
 int nngp_replicate_solve(nngp_ctx *ctx, const RepSpec &s) {
   if (s.nRep <= 0) return NNGP_OK;
+  if (s.m > 32) return nngp_fail(ctx, NNGP_ERR_ARG, "replicate solve: m > 32");
   const int n = s.n;
   const int64_t nI = std::max<int64_t>(nngp_nindx(n, s.m), 1);
-  LevelSchedule ls;
-  int st = nngp_level_schedule(ctx, n, s.nnIndx, s.nnLU, &ls);
-  if (st) return st;
+  int st = NNGP_OK;
   // samples per chunk: B, F and the location-major v of a chunk within a quarter of the free
   // memory (at most 32 GB)
   size_t freeb = 0, totalb = 0;
@@ -218,17 +137,23 @@ int nngp_replicate_solve(nngp_ctx *ctx, const RepSpec &s) {
   double *dF = (double *)nngp_malloc_async(ctx, sizeof(double) * (size_t)n * chunk);
   double *vbuf = (double *)nngp_malloc_async(ctx, sizeof(double) * (size_t)n * chunk);
   double *out = (double *)nngp_malloc_async(ctx, sizeof(double) * 2 * (size_t)chunk);
+  int *ready = (int *)nngp_malloc_async(ctx, sizeof(int) * (size_t)n);
+  int *words = (int *)nngp_malloc_async(ctx, sizeof(int) * 2);  // ticket, error bits
   auto release = [&]() {
     nngp_free_async(ctx, dB);
     nngp_free_async(ctx, dF);
     nngp_free_async(ctx, vbuf);
     nngp_free_async(ctx, out);
-    nngp_level_schedule_free(ctx, &ls);
+    nngp_free_async(ctx, ready);
+    nngp_free_async(ctx, words);
   };
-  if (!dB || !dF || !vbuf || !out) {
+  if (!dB || !dF || !vbuf || !out || !ready || !words) {
     release();
     return nngp_fail(ctx, NNGP_ERR_NO_MEMORY, "device allocation failed");
   }
+  // one block of four warps per SM: about five levels' worth of locations in flight at
+  // n = 1e6, so a warp seldom waits and few poll at once
+  const int grid = ctx->sm_count > 0 ? ctx->sm_count : 1;
   for (int r0 = 0; !st && r0 < s.nRep; r0 += chunk) {
     const int ns = std::min(chunk, s.nRep - r0);
     std::vector<BFData> datas(ns);
@@ -257,18 +182,27 @@ int nngp_replicate_solve(nngp_ctx *ctx, const RepSpec &s) {
     a.r0 = r0;
     a.nnIndx = s.nnIndx;
     a.nnLU = s.nnLU;
-    a.order = ls.order;
     a.B = dB;
     a.nI = nI;
     a.F = dF;
     a.z = s.z;
     a.zoff = s.d_zoff;
     a.vbuf = vbuf;
-    for (int l = 0; l < ls.depth; l++) {
-      const int lo = ls.start[l], cnt = ls.start[l + 1] - lo;
-      rep_level_kernel<<<(unsigned)nblocks((long long)cnt * ns, 128), 128, 0, ctx->stream>>>(a, lo, cnt);
+    if (cudaMemsetAsync(ready, 0, sizeof(int) * (size_t)n, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(words, 0, sizeof(int) * 2, ctx->stream) != cudaSuccess) {
+      st = nngp_fail(ctx, NNGP_ERR_CUDA, "replicate solve: memset failed");
+      break;
     }
-    ctx->launches += ls.depth;
+    rep_flow_kernel<<<grid, 32 * kFlowWarps, 0, ctx->stream>>>(a, ready, words);
+    ctx->launches++;
+    int herr[2] = {};
+    cudaMemcpyAsync(herr, words, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) == cudaSuccess && herr[1] != 0) {
+      st = nngp_fail(ctx, herr[1] & 1 ? NNGP_ERR_ARG : NNGP_ERR_CUDA,
+                     herr[1] & 1 ? "nnIndx lists a neighbor that is not a predecessor"
+                                 : "replicate solve: a wait for a neighbor timed out");
+      break;
+    }
     rep_finish_kernel<<<(unsigned)nblocks((long long)n * ns, 256), 256, 0, ctx->stream>>>(
         a, s.p, s.X, s.beta, s.bs_r, s.bs_j, s.xb_first, s.yRep);
     ctx->launches++;

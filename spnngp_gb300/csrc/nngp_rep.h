@@ -1,19 +1,9 @@
-// Level-scheduled replicate solve (nngp_rep.cu): the neighbor DAG's level schedule and the
-// batched draw y_rep = X beta + (I - B)^-1 F^(1/2) z for many parameter sets.
+// Replicate solve (nngp_rep.cu): the batched draw y_rep = X beta + (I - B)^-1 F^(1/2) z for
+// many parameter sets, by a dataflow triangular solve over the neighbor DAG.
 #pragma once
 
 #include <vector>
 #include "nngp_internal.h"
-
-// Locations sorted by level of the neighbor DAG: order[start[l] .. start[l + 1]) are the
-// locations whose longest neighbor chain has l links.
-struct LevelSchedule {
-  int n = 0, depth = 0;
-  int *order = nullptr;    // device, n
-  std::vector<int> start;  // host, depth + 1
-};
-int nngp_level_schedule(nngp_ctx *ctx, int n, const int *nnIndx, const int *nnLU, LevelSchedule *ls);
-void nngp_level_schedule_free(nngp_ctx *ctx, LevelSchedule *ls);
 
 // nRep replicates of one dataset (all pointers device memory).  Replicate r uses parameter set
 // d_theta[r], coefficients beta[r bs_r + j bs_j] (j < p), normals z[d_zoff[r] + i] (i < n), and

@@ -125,9 +125,9 @@ def test_rNNGPReplicated_matches_reference(sp, golden):
 
 @pytest.mark.parametrize("model,theta", [(0, (1.0, 0.1, 6.0)), (2, (1.0, 0.2, 12.0, 1.5))])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32r", 1e-6)])
-def test_rNNGPReplicated_level_schedule_matches_oracle(sp, orc, model, theta, precision, tol):
-    """The level-scheduled solve (one launch per level of the neighbor DAG over every sample)
-    against the oracle's sequential recurrence at a size with ~1200 levels."""
+def test_rNNGPReplicated_dataflow_solve_matches_oracle(sp, orc, model, theta, precision, tol):
+    """The dataflow solve (warps take locations in index order and wait for their neighbors)
+    against the oracle's sequential recurrence at a size whose neighbor DAG has ~1200 levels."""
     rng = np.random.default_rng(71)
     n, m, p, nS = 20000, 15, 2, 6
     c = xorder(rng.uniform(size=(n, 2)))
@@ -143,8 +143,26 @@ def test_rNNGPReplicated_level_schedule_matches_oracle(sp, orc, model, theta, pr
     assert np.max(np.abs(r["y.rep.samples"] - yo)) <= tol * max(1.0, np.max(np.abs(yo)))
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32r", 1e-6)])
+def test_rNNGPReplicated_unordered_locations_match_oracle(sp, orc, precision, tol):
+    """Locations in no spatial order (brute-force neighbor lists): index order is still a
+    topological order of the neighbor DAG, so the dataflow solve needs no ordering."""
+    rng = np.random.default_rng(74)
+    n, m, p, nS = 3000, 10, 2, 3
+    c = rng.uniform(size=(n, 2))
+    X = np.column_stack([np.ones(n), rng.normal(size=n)])
+    o = orc.mkNNIndx(cm(c), m)
+    th = np.array([1.0, 0.1, 6.0])[:, None] * rng.uniform(0.8, 1.25, size=(3, nS))
+    beta = rng.normal(size=(nS, p))
+    z = rng.normal(size=n * nS)
+    r = sp.rNNGPReplicated(X, m, c, 0, o[0], o[2], beta, th, z, precision=precision)
+    yo, st = orc.rNNGPReplicated(cm(X), m, cm(c), 0, o[0], o[2], beta, cm(th), z)
+    assert st == 0
+    assert np.max(np.abs(r["y.rep.samples"] - yo)) <= tol * max(1.0, np.max(np.abs(yo)))
+
+
 def test_rNNGPReplicated_rejects_non_predecessor_neighbors(sp, orc):
-    """A neighbor list naming a later location is refused by the level schedule's own check."""
+    """A neighbor list naming a later location is refused by the replicate solve's own check."""
     rng = np.random.default_rng(72)
     n, m = 500, 10
     c = xorder(rng.uniform(size=(n, 2)))
