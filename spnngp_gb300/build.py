@@ -40,7 +40,7 @@ VARIANTS = {
     "nngp_bfr_inst.cu": [(f"_m{m}_c{c}", [f"-DBFR_M={m}", f"-DBFR_COV={c}"])
                          for m in (10, 15, 16) for c in (0, 1, 2, 3, 4)],
     "nngp_bfw_inst.cu": [(f"_m{m}_c{c}", [f"-DBFW_M={m}", f"-DBFW_COV={c}"])
-                         for m in (24, 32) for c in (0, 1, 2, 3, 4)],
+                         for m in (20, 24, 32) for c in (0, 1, 2, 3, 4)],
     "nngp_bfdf_inst.cu": [(f"_m{m}_c{c}", [f"-DBFDF_M={m}", f"-DBFDF_COV={c}"])
                           for m in (16, 24) for c in (0, 1, 2, 3, 4)],
     "nngp_bfwdf_inst.cu": [(f"_m{m}_c{c}", [f"-DBFWDF_M={m}", f"-DBFWDF_COV={c}"])

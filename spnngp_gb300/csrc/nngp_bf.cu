@@ -181,6 +181,9 @@ int warp_call_m(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int gr
 }
 int warp_call(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb = 4, int grid = 0, bool query_occ = false) {
   const bool m1 = pl->mode == 1;
+  if (pl->mmax <= 20)
+    return m1 ? warp_call_m<20, 1>(ctx, pl, t0, t1, wpb, grid, query_occ)
+              : warp_call_m<20, 0>(ctx, pl, t0, t1, wpb, grid, query_occ);
   if (pl->mmax <= 24)
     return m1 ? warp_call_m<24, 1>(ctx, pl, t0, t1, wpb, grid, query_occ)
               : warp_call_m<24, 0>(ctx, pl, t0, t1, wpb, grid, query_occ);
@@ -346,7 +349,7 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
 // default shape (4 warps, one tile per warp).
 int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   std::string key = tune_key(pl, t1 - t0);  // "M=<reg_m> ...": the warp kernel's bound instead
-  key = "warp M=" + std::to_string(pl->mmax <= 24 ? 24 : 32) + key.substr(key.find(' '));
+  key = "warp M=" + std::to_string(pl->mmax <= 20 ? 20 : pl->mmax <= 24 ? 24 : 32) + key.substr(key.find(' '));
   auto grid_of = [&](int wpb, int gm, int ntiles) {
     const int full = (ntiles + wpb - 1) / wpb;
     if (gm <= 0) return full;

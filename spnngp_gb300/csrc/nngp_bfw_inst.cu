@@ -1,5 +1,5 @@
 // Explicit instantiations of the warp-per-location FP32R B/F kernel (nngp_bfw_kernel.cuh) for
-// one neighbor bound BFW_M (24 or 32) and correlation code BFW_COV (NNGP_COV_*), both modes.
+// one neighbor bound BFW_M (20, 24 or 32) and correlation code BFW_COV (NNGP_COV_*), both modes.
 // The build compiles this file once per variant, in parallel.
 #include "nngp_bfw_kernel.cuh"
 #if !defined(BFW_M) || !defined(BFW_COV)

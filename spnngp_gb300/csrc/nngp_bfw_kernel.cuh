@@ -1,4 +1,4 @@
-// FP32R B/F kernel for neighbor bounds 16 < m <= 32 (M = 24, 32): one warp per location
+// FP32R B/F kernel for neighbor bounds 16 < m <= 32 (M = 20, 24, 32): one warp per location
 // (reference updateBF, src/rNNGP.cpp:46-101; updateConjBF, src/cNNGP.cpp:24-69; the
 // likelihood sums of src/rNNGP.cpp:306-317 and Q, src/util.cpp:261-280).
 //

@@ -269,7 +269,8 @@ def test_warp_kernel_tuning_keeps_results(sp, m):
     B1, F1, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, "fp32r", ctx=ctx)
     ld1, G1 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, "fp32r", ctx=ctx)
     rep = ctx.autotune_report()
-    keys = [k for k in rep if k.startswith(f"warp M={24 if m <= 24 else 32} ")]
+    bound = 20 if m <= 20 else 24 if m <= 24 else 32  # the warp kernel's instantiated bounds
+    keys = [k for k in rep if k.startswith(f"warp M={bound} ")]
     assert len(keys) == 2  # the standalone and the fused mode
     for k in keys:
         assert rep[k]["wpb"] in (1, 2, 4) and len(rep[k]["candidates"]) >= 3
