@@ -252,6 +252,32 @@ def test_double_float_tier_on_ill_conditioned_gaussian(sp, orc, m, phi):
     assert abs(ll["fp32r"] - ll["fp64"]) <= 1e-6 * abs(ll["fp64"])
 
 
+@pytest.mark.parametrize("m", [15, 20, 32])
+@pytest.mark.parametrize("model,theta", [("spherical", (1.0, 1e-7, 0.8)), ("matern", (1.0, 1e-5, 2.0, 2.3))])
+def test_double_float_tier_scalar_covariance_paths(sp, m, model, theta):
+    """The double-float re-solve on the covariance paths without a packed form: spherical and
+    Matern with a general nu (K_nu evaluated in FP64), long ranges and small nuggets, so the
+    float factor cannot be certified (F stays above 1e-6 (sigma^2 + tau^2), the double-float
+    tier's floor); F, B and the log-likelihood against the FP64 form."""
+    c, X, y = dataset(6000, 900 + m)
+    ctx = sp.default_context()
+    nb = sp.mkNNIndxCB(c, m)
+    nn, lu = nb["nnIndx"], nb["nnIndxLU"]
+    B64, F64, _ = sp.updateBF(c, nn, lu, m, model, theta, "fp64")
+    B32, F32, _ = sp.updateBF(c, nn, lu, m, model, theta, "fp32r")
+    n_df, n_64 = ctx.fp32r_tiers()
+    assert n_df > 0.25 * len(c), (n_df, n_64)  # the tier under test took a good share
+    assert float(np.max(np.abs(F32 - F64) / F64)) <= TOL_F
+    assert float(np.max(np.abs(B32 - B64))) <= TOL_B * max(1.0, float(np.max(np.abs(B64))))
+    V = np.column_stack([X, y])
+    beta = np.array([1.0, -0.5])
+    ll = {}
+    for prec in ("fp64", "fp32r"):
+        ld, G = sp.loglik_gram(c, nn, lu, m, V, model, theta, prec)
+        ll[prec] = loglik(ld, G, beta)
+    assert abs(ll["fp32r"] - ll["fp64"]) <= TOL_LOGLIK * abs(ll["fp64"])
+
+
 @pytest.mark.parametrize("m", [20, 32])
 def test_warp_kernel_tuning_keeps_results(sp, m):
     """The warp-per-location kernel (16 < m <= 32) is tuned on its first large pass (1, 2 or 4
