@@ -57,22 +57,10 @@ __global__ void count_flags_kernel(const unsigned char *__restrict__ flags, size
   if (c) atomicAdd(out, c);
 }
 
-// Sum over the 256 threads of a block, in a fixed tree order (every thread gets the sum).
-__device__ double block_sum256(double x, double *sbuf) {
-  sbuf[threadIdx.x] = x;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w) sbuf[threadIdx.x] += sbuf[threadIdx.x + w];
-    __syncthreads();
-  }
-  const double r = sbuf[0];
-  __syncthreads();
-  return r;
-}
-
 // Fixed-order reduction of per-tile partials in two levels.  Level 1: block (job, b) sums
 // tiles [b C, (b + 1) C) of the job (C = kReduceChunk); thread t sums tiles t, t + 256, ... of
-// the chunk, value by value in order, then a fixed tree over the threads.  Values are taken
+// the chunk, value by value in order, then a fixed binary tree over the 256 threads (pairs
+// t, t + w for w = 128, 64, ..., 1), every value's tree in the same barriers.  Values are taken
 // eight at a time so each thread reads whole rows of the tile-major partial array
 // (contiguous across the warp).  With jobs_fb, the FP64 re-solve's partials of the tiles marked
 // in fb_marks are summed the same way into a second slot (skipped when no tile was recorded:
@@ -85,7 +73,7 @@ __global__ void reduce_chunks_kernel(const BFJob *__restrict__ jobs, const BFJob
                                      int ng, int nchunks, double *__restrict__ out2) {
   const int jid = blockIdx.x / nchunks, b = blockIdx.x % nchunks;
   const BFJob job = jobs[jid];
-  __shared__ double sbuf[256];
+  __shared__ double sbuf16[16][256];
   const bool any_fb = jobs_fb && *fb_count > 0;
   double *o = out2 + (size_t)blockIdx.x * 2 * ng;
   const int t0 = b * kReduceChunk;
@@ -111,15 +99,27 @@ __global__ void reduce_chunks_kernel(const BFJob *__restrict__ jobs, const BFJob
           if (v0 + j < ng) accf[j] += row[j];
       }
     }
-#pragma unroll 1
-    for (int j = 0; j < 8 && v0 + j < ng; j++) {
-      const double s = block_sum256(acc[j], sbuf);
-      const double sf = jobs_fb ? block_sum256(accf[j], sbuf) : 0.0;
-      if (threadIdx.x == 0) {
-        o[v0 + j] = s;
-        o[ng + v0 + j] = sf;
-      }
+    // the sixteen trees (eight values, main and re-solve sums) side by side: per value the
+    // order of block_sum256, one barrier per level for all of them
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      sbuf16[j][threadIdx.x] = acc[j];
+      sbuf16[8 + j][threadIdx.x] = accf[j];
     }
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) sbuf16[j][threadIdx.x] += sbuf16[j][threadIdx.x + w];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x < 8 && v0 + (int)threadIdx.x < ng) {
+      const int j = threadIdx.x;
+      o[v0 + j] = sbuf16[j][0];
+      o[ng + v0 + j] = jobs_fb ? sbuf16[8 + j][0] : 0.0;
+    }
+    __syncthreads();
   }
 }
 
@@ -128,10 +128,24 @@ __global__ void reduce_final_kernel(const double *__restrict__ out2, int ng, int
   const int jid = blockIdx.x;
   for (int v = threadIdx.x; v < ng; v += blockDim.x) {
     double s = 0.0, sf = 0.0;
-    for (int b = 0; b < nchunks; b++) {
-      const double *o = out2 + ((size_t)jid * nchunks + b) * 2 * ng;
-      s += o[v];
-      sf += o[ng + v];
+    const double *o = out2 + (size_t)jid * nchunks * 2 * ng + v;
+    int b = 0;
+    for (; b + 8 <= nchunks; b += 8) {  // eight chunks' loads in flight, added in chunk order
+      double x[8], xf[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        x[u] = o[(size_t)(b + u) * 2 * ng];
+        xf[u] = o[(size_t)(b + u) * 2 * ng + ng];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        s += x[u];
+        sf += xf[u];
+      }
+    }
+    for (; b < nchunks; b++) {
+      s += o[(size_t)b * 2 * ng];
+      sf += o[(size_t)b * 2 * ng + ng];
     }
     out[(size_t)jid * ng + v] = with_fb ? s + sf : s;
   }
