@@ -944,7 +944,8 @@ def run_ours(args):
             "dtype": "f32+f64", "data": "synthetic",
             "config": bench_config(),
             "form": "FP32 covariance build and Cholesky, one double-float (Dot2) residual refinement; "
-                    "FP64 re-solve of the locations the error estimate flags",
+                    "locations the error estimate flags re-solved in double-float (FP64 where that "
+                    "cannot certify them)",
             "fp64_form": {"value": N / (ms64 * 1e-3), "ms_per_step": ms64, "kernel_ms": kms64},
             "fp32r_over_fp64": ms64 / ms32,
             "loglik_rel_err_fp32r_vs_fp64": abs(ll32 - ll64) / abs(ll64),

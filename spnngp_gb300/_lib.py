@@ -214,7 +214,8 @@ class Context:
         return int(a.value), int(b.value)
 
     def fp32r_resolved(self) -> tuple[int, int]:
-        """(locations re-solved in FP64, locations covered) of the last single-dataset FP32R pass."""
+        """(locations re-solved in higher precision -- double-float or FP64 --, locations covered)
+        of the last single-dataset FP32R pass."""
         r, n = _i64(), _i64()
         self.call("nngp_fp32r_resolved", C.byref(r), C.byref(n))
         return int(r.value), int(n.value)
