@@ -1,13 +1,14 @@
-// Double-float re-solve of the locations the FP32R register kernel (m <= 16,
-// nngp_bfr_kernel.cuh) flags -- a float pivot failed or the float solve's error estimate was
-// too large, typically a gaussian covariance with a small nugget (condition numbers ~1e7).
+// Double-float re-solve of the locations the FP32R kernels flag for m <= 24 (the register
+// kernel, nngp_bfr_kernel.cuh, and the warp kernel's 20- and 24-row forms,
+// nngp_bfw_kernel.cuh) -- a float pivot failed or the float solve's error estimate was too
+// large, typically a gaussian covariance with a small nugget (condition numbers ~1e7).
 // Instead of handing them all to the FP64 kernel, whose pipe runs at 1/64 of the FP32 rate on
 // GB300, this kernel solves them in double-float arithmetic (about 48-bit significands) on
 // the FP32 pipe (reference updateBF, src/rNNGP.cpp:46-101, and the likelihood sums of
 // src/rNNGP.cpp:306-317; the double-float arithmetic of nngp_df.cuh, the covariance of
 // nngp_cov_df.cuh):
 //   1. neighbor offsets from the split coordinates as double-float pairs on a common grid
-//      (as the register kernel), the covariance c and the lower triangle of C in double-float;
+//      (as the FP32R kernels), the covariance c and the lower triangle of C in double-float;
 //   2. the Cholesky factor of the augmented matrix [C c; c' S] (S = sigma^2 + tau^2) in
 //      double-float, right-looking (outer-product form): its last row is z = L^-1 c and its
 //      last pivot is F = S - z'z, the quantity NNGP needs (accurate where F is a small
@@ -26,8 +27,9 @@
 // evaluated two at a time.  (A row-by-row factorization with compensated dot products issued
 // about one instruction at a time; fully unrolling the factorization per neighbor bound cut
 // the instruction count by 40 % but overflowed the instruction cache.)
-// The kernel walks the FP32R pass's list of flagged FP64 tiles (64 locations each, the FP64
-// kernel's tile) and solves every flagged location of a tile.  A location it cannot certify --
+// The kernel walks the FP32R pass's list of flagged FP64 tiles (the FP64 kernel's tile: 64
+// locations up to 16 neighbors, 32 beyond; one tile per block) and solves every flagged
+// location of a tile.  A location it cannot certify --
 // a non-positive double-float pivot, F < 1e-6 (sigma^2 + tau^2), or a squared pivot ratio (a
 // lower bound of the condition number) above 1e10 -- sends its whole tile on to the FP64
 // kernel (a second list), so every tile's partial sums come from one kernel and keep their
