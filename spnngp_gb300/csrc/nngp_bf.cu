@@ -633,8 +633,8 @@ int nngp_bf_primary(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
 int nngp_bf_finish(nngp_ctx *ctx, const BFPlan *pl, double *d_out) {
   int st;
   const bool fp32r = pl->precision == NNGP_FP32R;
-  // FP32R: the re-solve of the recorded tiles (register-kernel plans: double-float first, FP64
-  // for the tiles it cannot certify), folded into the same fixed-order sums
+  // FP32R: the re-solve of the recorded tiles (double-float first, FP64 for the tiles it
+  // cannot certify), folded into the same fixed-order sums
   if (fp32r && (st = launch_df_any(ctx, pl))) return st;
   if (fp32r && (st = launch_pass(ctx, pl, false, true, 0, 0))) return st;
   reduce_chunks_kernel<<<pl->njobs * pl->red_chunks, 256, 0, ctx->stream>>>(

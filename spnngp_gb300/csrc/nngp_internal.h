@@ -238,9 +238,8 @@ struct BFPlan {
   // FP32R: [count | marks (tiles_fb)] words and the list of FP64 tiles to re-solve
   unsigned *d_fb_words = nullptr;
   int *d_fb_list = nullptr;
-  // the tiles the FP64 kernel re-solves: the list above, or (register-kernel plans, whose
-  // flagged tiles go to the double-float kernel first) the tiles that kernel could not certify,
-  // with the number of flagged locations in them
+  // the tiles the FP64 kernel re-solves: those the double-float kernel (which walks the list
+  // above first) could not certify, with the number of flagged locations in them
   int *d_fb64_list = nullptr;
   int *d_fb64_count = nullptr;
   unsigned long long *d_fb64_locs = nullptr;
