@@ -147,6 +147,15 @@ __global__ void __launch_bounds__(256, 1) bfr_kernel(const BFData *__restrict__ 
       off = d.nnLU[i];
       mi = min(d.nnLU[d.n + i], M);
     }
+    if constexpr (COV == NNGP_COV_GAU || COV == NNGP_COV_ANY) {
+      if (nngp_route_double_float(*cpp)) {  // the job's parameter set: warp-uniform
+        // every location to the double-float re-solve, nothing from the float factor here
+        if (active) nngp_flag_for_fp64(job, i);
+        const int ngz = MODE == 0 ? 1 : 1 + nv * (nv + 1) / 2;
+        for (int t = lane; t < ngz; t += 32) job.partial[(size_t)tj * ngz + t] = 0.0;
+        continue;
+      }
+    }
     const CorDF ck = cor_prepare<COV>(cpp);
     const F::df Sd{cpp->dfDiag[0], cpp->dfDiag[1]};  // the diagonal sigma^2 + tau^2
     fill_tab<COV>(tab, ck, cpp, lane);  // the warp's exp table and Matern coefficients

@@ -110,6 +110,16 @@ __global__ void __launch_bounds__(128, 4) bfw_kernel(const BFData *__restrict__ 
     const BFData *dp = datas + jp->data;
     const CovParams *cpp = thetas + jp->theta;
     const int tj = tile - jp->tile0;
+    if constexpr (COV == NNGP_COV_GAU || COV == NNGP_COV_ANY) {
+      if (nngp_route_double_float(*cpp)) {  // the job's parameter set: warp-uniform
+        // every location to the double-float re-solve, nothing from the float factor here
+        if (tj * 32 + lane < dp->n) nngp_flag_for_fp64(*jp, tj * 32 + lane);
+        double *partial = jp->partial + (size_t)tj * ng;
+        if (lane < ng) partial[lane] = 0.0;
+        if (lane + 32 < ng) partial[lane + 32] = 0.0;
+        continue;
+      }
+    }
     const CorDF ck = nngp_bfr::cor_prepare<COV>(cpp);
     const F::df Sd{cpp->dfDiag[0], cpp->dfDiag[1]};  // the diagonal sigma^2 + tau^2
     nngp_bfr::fill_tab<COV>(tab, ck, cpp, lane);  // the warp's exp table and Matern coefficients

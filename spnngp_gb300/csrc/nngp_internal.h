@@ -127,6 +127,15 @@ struct CovParams {
   float dfPoly[9][2];
 };
 
+// Parameter sets whose FP32R pass hands every location to the double-float re-solve without
+// trying the float factor: a gaussian covariance (model code 3) with a nugget at most 1e-4 of
+// sigma^2.  Its neighborhood systems have condition numbers of 1e4 and more, so the float
+// factor's error estimate flags essentially every location; the rule depends on the
+// parameters alone, so a location's result never depends on the batch or on earlier calls.
+__host__ __device__ inline bool nngp_route_double_float(const CovParams &c) {
+  return c.model == 3 && c.tauSq <= 1e-4 * c.sigmaSq;
+}
+
 __host__ __device__ inline void cov_split(double v, float (&out)[2]) {
   out[0] = (float)v;
   out[1] = (float)(v - (double)out[0]);
