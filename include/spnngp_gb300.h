@@ -288,8 +288,9 @@ int nngp_fp32r_resolved(nngp_ctx *ctx, int64_t *resolved, int64_t *locations);
  * solve could not certify).  Synchronises the context's stream. */
 int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);
 
-/* Launch-shape autotuner of the FP32R B/F kernel for m <= 16, no counterpart
- * in the reference (it stands in for the reference's n.omp.threads tuning).
+/* Launch-shape autotuner of the FP32R B/F kernels, no counterpart in the
+ * reference (it stands in for the reference's n.omp.threads tuning).  For the
+ * register kernel (m <= 16):
  * The first pass of a (neighbor bound, mode, correlation model, size class)
  * times every candidate shape -- warps per block 1-6 (8) with the covariance
  * kept in shared memory, or 4 / 8 with its low-order parts in the SM's tensor
@@ -305,8 +306,8 @@ int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);
  * writes one line per tuned class ("key: wpb=W grid_mode=G tmem=T ms=X |
  * WxBLOCKS[t]:ms ...", one entry per candidate, t marking tensor memory) into
  * buf and returns the number of classes.  The warp-per-location FP32R kernel
- * (16 < m <= 32) is tuned the same way over 1, 2 or 4 warps per block (classes
- * "warp M=24|32 ..."). */
+ * (16 < m <= 32) is tuned the same way over 1, 2 or 4 warps per block, one tile
+ * per warp or a persistent grid (classes "warp M=20|24|32 ..."). */
 int nngp_set_autotune(nngp_ctx *ctx, int on);
 int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode, int use_tmem);
 int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len);
