@@ -51,7 +51,8 @@ typedef enum {
 
 typedef enum {
   NNGP_FP64 = 0,  /* plain FP64 throughout */
-  NNGP_FP32R = 1  /* FP32 covariance build + Cholesky, one FP64-residual refinement of B */
+  NNGP_FP32R = 1  /* FP32 Cholesky + one refinement against the covariance in double-float;
+                     locations it cannot certify re-solved in double-float, then FP64 */
 } nngp_precision;
 
 /* ---------------------------------------------------------------- context */
