@@ -35,7 +35,9 @@ int occupancy_warp(int wpb);
 }  // namespace nngp_bfw
 namespace nngp_bfwd {
 template <int M, int MODE, int COV>
-int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1);
+int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1, int wpb, int grid);
+template <int M, int MODE, int COV>
+int occupancy_warp_d(int wpb);
 }  // namespace nngp_bfwd
 namespace nngp_bfdf {
 template <int M, int MODE, int COV>
@@ -154,6 +156,7 @@ __global__ void reduce_final_kernel(const double *__restrict__ out2, int ng, int
 }  // namespace
 
 namespace {
+int run_warp_d(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1);
 // The FP64 kernel: the FP64 form's primary pass, or the re-solve of the locations an FP32R
 // pass flagged (fallback_pass)
 template <int MODE, int COV>
@@ -162,7 +165,9 @@ int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, i
   // 24-neighbor bound: the thread-per-location kernel still holds two blocks per SM and beats the
   // warp form (38 against 67 ms at n = 1e6); at 32 the warp form wins (97 against 206 ms)
   if (pl->mmax <= 24) return launch_one<24, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
-  return nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
+  // the primary pass in its tuned shape, the re-solve of recorded tiles in the default one
+  if (fallback_pass) return nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, true, 0, 0, 4, 0);
+  return run_warp_d(ctx, pl, t0, t1);
 }
 
 template <int MODE>
@@ -356,18 +361,18 @@ int run_reg(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   return reg_call(ctx, pl, wpb, reg_grid(ctx, pl, wpb, gm, t1 - t0, tm), false, t0, t1, tm);
 }
 
-// Launch shape of the warp-per-location FP32R kernel, tuned like the register kernel's: warps per
-// block 1, 2 or 4, each with one tile per warp or a persistent grid of 1 or 2 x resident blocks
-// x SMs, timed on the plan's own tiles (at most kTuneSampleTiles) on its first pass of a size
-// class; passes under stream capture or of fewer than kTuneMinTiles tiles use the tuned or the
-// default shape (4 warps, one tile per warp).
-int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
-  std::string key = tune_key(pl, t1 - t0);  // "M=<reg_m> ...": the warp kernel's bound instead
-  key = "warp M=" + std::to_string(pl->mmax <= 20 ? 20 : pl->mmax <= 24 ? 24 : 32) + key.substr(key.find(' '));
+// Launch shape of a warp-per-location kernel, tuned like the register kernel's: warps per
+// block 1, 2 or 4, each with one tile per warp or a persistent grid of 1 or 2 x resident
+// blocks x SMs, timed on the plan's own tiles (at most kTuneSampleTiles) on its first pass of
+// a size class; passes under stream capture or of fewer than kTuneMinTiles tiles use the tuned
+// or the default shape (4 warps, one tile per warp).  call(t0, t1, wpb, grid) launches the
+// kernel, occ(wpb) returns its blocks per SM (0: that block size cannot run).
+template <class Call, class Occ>
+int run_tuned_warps(nngp_ctx *ctx, const std::string &key, int t0, int t1, Call call, Occ occ) {
   auto grid_of = [&](int wpb, int gm, int ntiles) {
     const int full = (ntiles + wpb - 1) / wpb;
     if (gm <= 0) return full;
-    const long cap = (long)gm * warp_call(ctx, pl, 0, 0, wpb, 0, true) * (ctx->sm_count > 0 ? ctx->sm_count : 1);
+    const long cap = (long)gm * occ(wpb) * (ctx->sm_count > 0 ? ctx->sm_count : 1);
     return (int)(cap < full ? (cap > 0 ? cap : 1) : full);
   };
   auto it = ctx->tuned.find(key);
@@ -383,14 +388,14 @@ int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
       NNGP_CUDA_TRY(ctx, cudaEventCreate(&e1));
       int st = NNGP_OK;
       for (int wpb : {1, 2, 4}) {
-        if (warp_call(ctx, pl, 0, 0, wpb, 0, true) <= 0) continue;
+        if (occ(wpb) <= 0) continue;
         const int full = grid_of(wpb, 0, s1 - t0);
         for (int gm : {0, 1, 2}) {
           const int grid = grid_of(wpb, gm, s1 - t0);
           if (gm > 0 && grid >= full) continue;
-          if ((st = warp_call(ctx, pl, t0, s1, wpb, grid))) break;  // warm-up
+          if ((st = call(t0, s1, wpb, grid))) break;  // warm-up
           cudaEventRecord(e0, ctx->stream);
-          if ((st = warp_call(ctx, pl, t0, s1, wpb, grid))) break;
+          if ((st = call(t0, s1, wpb, grid))) break;
           cudaEventRecord(e1, ctx->stream);
           if (cudaEventSynchronize(e1) != cudaSuccess) {
             st = nngp_fail(ctx, NNGP_ERR_CUDA, "autotune: event synchronisation failed");
@@ -417,7 +422,43 @@ int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   }
   const int wpb = it != ctx->tuned.end() ? it->second.wpb : 4;
   const int gm = it != ctx->tuned.end() ? it->second.grid_mode : 0;
-  return warp_call(ctx, pl, t0, t1, wpb, grid_of(wpb, gm, t1 - t0));
+  return call(t0, t1, wpb, grid_of(wpb, gm, t1 - t0));
+}
+
+// The FP32R warp kernel (16 < m <= 32), tuning classes "warp M=20|24|32 ...".
+int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  std::string key = tune_key(pl, t1 - t0);  // "M=<reg_m> ...": the warp kernel's bound instead
+  key = "warp M=" + std::to_string(pl->mmax <= 20 ? 20 : pl->mmax <= 24 ? 24 : 32) + key.substr(key.find(' '));
+  return run_tuned_warps(
+      ctx, key, t0, t1, [&](int a, int b, int wpb, int grid) { return warp_call(ctx, pl, a, b, wpb, grid); },
+      [&](int wpb) { return warp_call(ctx, pl, 0, 0, wpb, 0, true); });
+}
+
+// The FP64 warp kernel (24 < m <= 32), tuning classes "fp64 warp M=32 ...".
+template <int MODE, int COV>
+int wd_call_c(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid, bool query_occ) {
+  return query_occ ? nngp_bfwd::occupancy_warp_d<32, MODE, COV>(wpb)
+                   : nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, false, t0, t1, wpb, grid);
+}
+template <int MODE>
+int wd_call_m(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid, bool query_occ) {
+  switch (pl->cov) {
+    case NNGP_COV_EXP: return wd_call_c<MODE, NNGP_COV_EXP>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    case NNGP_COV_SPH: return wd_call_c<MODE, NNGP_COV_SPH>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    case NNGP_COV_MAT_HALF: return wd_call_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    case NNGP_COV_GAU: return wd_call_c<MODE, NNGP_COV_GAU>(ctx, pl, t0, t1, wpb, grid, query_occ);
+    default: return wd_call_c<MODE, NNGP_COV_ANY>(ctx, pl, t0, t1, wpb, grid, query_occ);
+  }
+}
+int run_warp_d(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
+  std::string key = tune_key(pl, t1 - t0);
+  key = "fp64 warp M=32" + key.substr(key.find(' '));
+  auto call = [&](int a, int b, int wpb, int grid, bool q) {
+    return pl->mode == 1 ? wd_call_m<1>(ctx, pl, a, b, wpb, grid, q) : wd_call_m<0>(ctx, pl, a, b, wpb, grid, q);
+  };
+  return run_tuned_warps(
+      ctx, key, t0, t1, [&](int a, int b, int wpb, int grid) { return call(a, b, wpb, grid, false); },
+      [&](int wpb) { return call(0, 0, wpb, 0, true); });
 }
 
 template <int M>

@@ -6,6 +6,8 @@
 #error "nngp_bfwd_inst.cu is compiled once per variant with -DBFWD_M and -DBFWD_COV"
 #endif
 namespace nngp_bfwd {
-template int launch_warp_d<BFWD_M, 0, BFWD_COV>(nngp_ctx *, const BFPlan *, bool, int, int);
-template int launch_warp_d<BFWD_M, 1, BFWD_COV>(nngp_ctx *, const BFPlan *, bool, int, int);
+template int launch_warp_d<BFWD_M, 0, BFWD_COV>(nngp_ctx *, const BFPlan *, bool, int, int, int, int);
+template int occupancy_warp_d<BFWD_M, 0, BFWD_COV>(int);
+template int launch_warp_d<BFWD_M, 1, BFWD_COV>(nngp_ctx *, const BFPlan *, bool, int, int, int, int);
+template int occupancy_warp_d<BFWD_M, 1, BFWD_COV>(int);
 }  // namespace nngp_bfwd

@@ -202,31 +202,51 @@ __global__ void __launch_bounds__(128, 3) bfwd_kernel(const BFData *__restrict__
 }
 
 // Launches the kernel on tiles [t0, t1) of the plan's primary jobs, or (fallback_pass) on the
-// FP64 tiles the FP32R pass recorded: blocks of four warps, one 32-location tile per warp.
+// FP64 tiles the FP32R pass recorded: blocks of wpb (1 - 4) warps, `grid` blocks (0: one
+// 32-location tile per warp; fewer: each warp loops over tiles).  Each warp reduces its own
+// tiles, so the shape never changes a result.
 template <int M, int MODE, int COV>
-int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1) {
-  const size_t smem = sizeof(double) * kWarpDoubles * kWarpsPerBlock;
-  static bool configured[64] = {};  // the attribute is per device
+int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1, int wpb = kWarpsPerBlock,
+                  int grid = 0) {
+  static bool configured[64] = {};  // the attribute is per device (set for the largest block)
   const int dev = ctx->device & 63;
   if (!configured[dev]) {
     NNGP_CUDA_TRY(ctx, cudaFuncSetAttribute(bfwd_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem));
+                                            (int)(sizeof(double) * kWarpDoubles * kWarpsPerBlock)));
     configured[dev] = true;
   }
+  if (wpb < 1 || wpb > kWarpsPerBlock) wpb = kWarpsPerBlock;
+  const size_t smem = sizeof(double) * kWarpDoubles * wpb;
   const int tiles = fallback_pass ? pl->tiles_fb : t1 - t0;
   if (tiles <= 0) return NNGP_OK;
-  int grid = (tiles + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const int full = (tiles + wpb - 1) / wpb;
+  if (grid <= 0 || grid > full) grid = full;
   if (fallback_pass) {
     // the re-solve walks the recorded tiles (none recorded: every block returns at once)
     const int cap = 3 * (ctx->sm_count > 0 ? ctx->sm_count : 1);
     grid = grid < cap ? grid : cap;
   }
-  bfwd_kernel<M, MODE, COV><<<grid, 32 * kWarpsPerBlock, smem, ctx->stream>>>(
+  bfwd_kernel<M, MODE, COV><<<grid, 32 * wpb, smem, ctx->stream>>>(
       pl->d_datas, pl->d_thetas, fallback_pass ? pl->d_jobs_fb : pl->d_jobs, pl->njobs, fallback_pass ? 0 : t0,
       fallback_pass ? pl->tiles_fb : t1, pl->nv, pl->d_status, fallback_pass ? 1 : 0,
       fallback_pass ? pl->d_fb64_list : nullptr, fallback_pass ? (const int *)pl->d_fb64_count : nullptr);
   NNGP_LAUNCH_CHECK(ctx);
   return NNGP_OK;
+}
+
+// Blocks of wpb warps one SM holds at once (current device).
+template <int M, int MODE, int COV>
+int occupancy_warp_d(int wpb) {
+  int dev = 0, blocks = 0;
+  cudaGetDevice(&dev);
+  if (wpb < 1 || wpb > kWarpsPerBlock) return 0;
+  if (cudaFuncSetAttribute(bfwd_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(sizeof(double) * kWarpDoubles * kWarpsPerBlock)) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, bfwd_kernel<M, MODE, COV>, 32 * wpb,
+                                                    sizeof(double) * kWarpDoubles * wpb) != cudaSuccess)
+    return 0;
+  return blocks;
 }
 
 }  // namespace nngp_bfwd

@@ -278,25 +278,26 @@ def test_double_float_tier_scalar_covariance_paths(sp, m, model, theta):
     assert abs(ll["fp32r"] - ll["fp64"]) <= TOL_LOGLIK * abs(ll["fp64"])
 
 
-@pytest.mark.parametrize("m", [20, 32])
-def test_warp_kernel_tuning_keeps_results(sp, m):
-    """The warp-per-location kernel (16 < m <= 32) is tuned on its first large pass (1, 2 or 4
-    warps per block, one tile per warp or a persistent grid); the tuned shape gives bitwise the
-    results of the default shape."""
+@pytest.mark.parametrize("m,precision", [(20, "fp32r"), (32, "fp32r"), (32, "fp64")])
+def test_warp_kernel_tuning_keeps_results(sp, m, precision):
+    """The warp-per-location kernels (FP32R for 16 < m <= 32, FP64 for 24 < m <= 32) are tuned
+    on their first large pass (1, 2 or 4 warps per block, one tile per warp or a persistent
+    grid); the tuned shape gives bitwise the results of the default shape."""
     c, X, y = dataset(80_000, 500 + m)
     V = np.column_stack([X, y])
     ctx = sp.Context(0)
     nb = sp.mkNNIndxCB(c, m, ctx=ctx)
     theta = (1.0, 0.1, 8.0)
     ctx.call("nngp_set_autotune", 0)
-    B0, F0, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, "fp32r", ctx=ctx)
-    ld0, G0 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, "fp32r", ctx=ctx)
+    B0, F0, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, precision, ctx=ctx)
+    ld0, G0 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, precision, ctx=ctx)
     ctx.call("nngp_set_autotune", 1)
-    B1, F1, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, "fp32r", ctx=ctx)
-    ld1, G1 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, "fp32r", ctx=ctx)
+    B1, F1, _ = sp.updateBF(c, nb["nnIndx"], nb["nnIndxLU"], m, "exponential", theta, precision, ctx=ctx)
+    ld1, G1 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, precision, ctx=ctx)
     rep = ctx.autotune_report()
-    bound = 20 if m <= 20 else 24 if m <= 24 else 32  # the warp kernel's instantiated bounds
-    keys = [k for k in rep if k.startswith(f"warp M={bound} ")]
+    bound = 20 if m <= 20 else 24 if m <= 24 else 32  # the warp kernels' instantiated bounds
+    prefix = f"warp M={bound} " if precision == "fp32r" else f"fp64 warp M={bound} "
+    keys = [k for k in rep if k.startswith(prefix)]
     assert len(keys) == 2  # the standalone and the fused mode
     for k in keys:
         assert rep[k]["wpb"] in (1, 2, 4) and len(rep[k]["candidates"]) >= 3
