@@ -308,8 +308,7 @@ int nngp_fp32r_tiers(nngp_ctx *ctx, int64_t *double_float, int64_t *fp64);
  * WxBLOCKS[t]:ms ...", one entry per candidate, t marking tensor memory) into
  * buf and returns the number of classes.  The warp-per-location FP32R kernel
  * (16 < m <= 32) is tuned the same way over 1, 2 or 4 warps per block, one tile
- * per warp or a persistent grid (classes "warp M=20|24|32 ..."), and so is the
- * FP64 warp-per-location kernel for 24 < m <= 32 (classes "fp64 warp M=32 ..."). */
+ * per warp or a persistent grid (classes "warp M=20|24|32 ..."). */
 int nngp_set_autotune(nngp_ctx *ctx, int on);
 int nngp_set_launch_shape(nngp_ctx *ctx, int warps_per_block, int grid_mode, int use_tmem);
 int nngp_autotune_report(nngp_ctx *ctx, char *buf, int len);

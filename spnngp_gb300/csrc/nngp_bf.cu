@@ -36,8 +36,6 @@ int occupancy_warp(int wpb);
 namespace nngp_bfwd {
 template <int M, int MODE, int COV>
 int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, int t1, int wpb, int grid);
-template <int M, int MODE, int COV>
-int occupancy_warp_d(int wpb);
 }  // namespace nngp_bfwd
 namespace nngp_bfdf {
 template <int M, int MODE, int COV>
@@ -156,7 +154,6 @@ __global__ void reduce_final_kernel(const double *__restrict__ out2, int ng, int
 }  // namespace
 
 namespace {
-int run_warp_d(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1);
 // The FP64 kernel: the FP64 form's primary pass, or the re-solve of the locations an FP32R
 // pass flagged (fallback_pass)
 template <int MODE, int COV>
@@ -165,9 +162,7 @@ int launch_mode_c(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, i
   // 24-neighbor bound: the thread-per-location kernel still holds two blocks per SM and beats the
   // warp form (38 against 67 ms at n = 1e6); at 32 the warp form wins (97 against 206 ms)
   if (pl->mmax <= 24) return launch_one<24, MODE, COV>(ctx, pl, fallback_pass, t0, t1);
-  // the primary pass in its tuned shape, the re-solve of recorded tiles in the default one
-  if (fallback_pass) return nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, true, 0, 0, 4, 0);
-  return run_warp_d(ctx, pl, t0, t1);
+  return nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, fallback_pass, t0, t1, 4, 0);
 }
 
 template <int MODE>
@@ -432,33 +427,6 @@ int run_warp(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
   return run_tuned_warps(
       ctx, key, t0, t1, [&](int a, int b, int wpb, int grid) { return warp_call(ctx, pl, a, b, wpb, grid); },
       [&](int wpb) { return warp_call(ctx, pl, 0, 0, wpb, 0, true); });
-}
-
-// The FP64 warp kernel (24 < m <= 32), tuning classes "fp64 warp M=32 ...".
-template <int MODE, int COV>
-int wd_call_c(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid, bool query_occ) {
-  return query_occ ? nngp_bfwd::occupancy_warp_d<32, MODE, COV>(wpb)
-                   : nngp_bfwd::launch_warp_d<32, MODE, COV>(ctx, pl, false, t0, t1, wpb, grid);
-}
-template <int MODE>
-int wd_call_m(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1, int wpb, int grid, bool query_occ) {
-  switch (pl->cov) {
-    case NNGP_COV_EXP: return wd_call_c<MODE, NNGP_COV_EXP>(ctx, pl, t0, t1, wpb, grid, query_occ);
-    case NNGP_COV_SPH: return wd_call_c<MODE, NNGP_COV_SPH>(ctx, pl, t0, t1, wpb, grid, query_occ);
-    case NNGP_COV_MAT_HALF: return wd_call_c<MODE, NNGP_COV_MAT_HALF>(ctx, pl, t0, t1, wpb, grid, query_occ);
-    case NNGP_COV_GAU: return wd_call_c<MODE, NNGP_COV_GAU>(ctx, pl, t0, t1, wpb, grid, query_occ);
-    default: return wd_call_c<MODE, NNGP_COV_ANY>(ctx, pl, t0, t1, wpb, grid, query_occ);
-  }
-}
-int run_warp_d(nngp_ctx *ctx, const BFPlan *pl, int t0, int t1) {
-  std::string key = tune_key(pl, t1 - t0);
-  key = "fp64 warp M=32" + key.substr(key.find(' '));
-  auto call = [&](int a, int b, int wpb, int grid, bool q) {
-    return pl->mode == 1 ? wd_call_m<1>(ctx, pl, a, b, wpb, grid, q) : wd_call_m<0>(ctx, pl, a, b, wpb, grid, q);
-  };
-  return run_tuned_warps(
-      ctx, key, t0, t1, [&](int a, int b, int wpb, int grid) { return call(a, b, wpb, grid, false); },
-      [&](int wpb) { return call(0, 0, wpb, 0, true); });
 }
 
 template <int M>

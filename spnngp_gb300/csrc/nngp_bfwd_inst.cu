@@ -7,7 +7,5 @@
 #endif
 namespace nngp_bfwd {
 template int launch_warp_d<BFWD_M, 0, BFWD_COV>(nngp_ctx *, const BFPlan *, bool, int, int, int, int);
-template int occupancy_warp_d<BFWD_M, 0, BFWD_COV>(int);
 template int launch_warp_d<BFWD_M, 1, BFWD_COV>(nngp_ctx *, const BFPlan *, bool, int, int, int, int);
-template int occupancy_warp_d<BFWD_M, 1, BFWD_COV>(int);
 }  // namespace nngp_bfwd

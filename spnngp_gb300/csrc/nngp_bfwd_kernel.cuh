@@ -234,19 +234,4 @@ int launch_warp_d(nngp_ctx *ctx, const BFPlan *pl, bool fallback_pass, int t0, i
   return NNGP_OK;
 }
 
-// Blocks of wpb warps one SM holds at once (current device).
-template <int M, int MODE, int COV>
-int occupancy_warp_d(int wpb) {
-  int dev = 0, blocks = 0;
-  cudaGetDevice(&dev);
-  if (wpb < 1 || wpb > kWarpsPerBlock) return 0;
-  if (cudaFuncSetAttribute(bfwd_kernel<M, MODE, COV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(sizeof(double) * kWarpDoubles * kWarpsPerBlock)) != cudaSuccess)
-    return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, bfwd_kernel<M, MODE, COV>, 32 * wpb,
-                                                    sizeof(double) * kWarpDoubles * wpb) != cudaSuccess)
-    return 0;
-  return blocks;
-}
-
 }  // namespace nngp_bfwd

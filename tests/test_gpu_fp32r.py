@@ -278,11 +278,11 @@ def test_double_float_tier_scalar_covariance_paths(sp, m, model, theta):
     assert abs(ll["fp32r"] - ll["fp64"]) <= TOL_LOGLIK * abs(ll["fp64"])
 
 
-@pytest.mark.parametrize("m,precision", [(20, "fp32r"), (32, "fp32r"), (32, "fp64")])
+@pytest.mark.parametrize("m,precision", [(20, "fp32r"), (32, "fp32r")])
 def test_warp_kernel_tuning_keeps_results(sp, m, precision):
-    """The warp-per-location kernels (FP32R for 16 < m <= 32, FP64 for 24 < m <= 32) are tuned
-    on their first large pass (1, 2 or 4 warps per block, one tile per warp or a persistent
-    grid); the tuned shape gives bitwise the results of the default shape."""
+    """The warp-per-location FP32R kernel (16 < m <= 32) is tuned on its first large pass (1, 2
+    or 4 warps per block, one tile per warp or a persistent grid); the tuned shape gives
+    bitwise the results of the default shape."""
     c, X, y = dataset(80_000, 500 + m)
     V = np.column_stack([X, y])
     ctx = sp.Context(0)
@@ -296,7 +296,7 @@ def test_warp_kernel_tuning_keeps_results(sp, m, precision):
     ld1, G1 = sp.loglik_gram(c, nb["nnIndx"], nb["nnIndxLU"], m, V, "exponential", theta, precision, ctx=ctx)
     rep = ctx.autotune_report()
     bound = 20 if m <= 20 else 24 if m <= 24 else 32  # the warp kernels' instantiated bounds
-    prefix = f"warp M={bound} " if precision == "fp32r" else f"fp64 warp M={bound} "
+    prefix = f"warp M={bound} "
     keys = [k for k in rep if k.startswith(prefix)]
     assert len(keys) == 2  # the standalone and the fused mode
     for k in keys:
